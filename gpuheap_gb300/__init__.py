@@ -1,0 +1,278 @@
+"""gpuheap_gb300: a GB300-native batched priority queue (BGPQ).
+
+Host-side mirror of the reference's `Heap<K>` (ruadapt/gpuheap,
+heap/{tditdd,tditdd_np,buitdd,buitdd_np}/heap.cuh) over the C ABI of
+libgpuheap_gb300.so (include/gpuheap.h).  Device buffers are torch CUDA
+tensors (or anything with .data_ptr()); torch is only plumbing here.
+
+The reference picks the variant by include path; here it is an argument:
+    variant="topdown"  + partial_buffer=True   == tditdd
+    variant="topdown"  + partial_buffer=False  == tditdd_np
+    variant="bottomup" + partial_buffer=True   == buitdd
+    variant="bottomup" + partial_buffer=False  == buitdd_np
+
+The library is required: importing works without it, but every call raises
+if libgpuheap_gb300.so cannot be loaded (there is no CPU fallback).
+"""
+import ctypes
+import os
+
+__all__ = ["Heap", "HeapError", "KEY_KINDS", "lib", "library_path", "build"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+library_path = os.path.join(_HERE, "libgpuheap_gb300.so")
+
+KEY_KINDS = {"u32": 0, "i32": 1, "u64": 2}
+_KEY_BYTES = {"u32": 4, "i32": 4, "u64": 8}
+_KEY_CTYPE = {"u32": ctypes.c_uint32, "i32": ctypes.c_int32, "u64": ctypes.c_uint64}
+_VARIANTS = {"topdown": 0, "td": 0, "bottomup": 1, "bu": 1}
+
+GH_OK, GH_ERR_INVALID, GH_ERR_CAPACITY, GH_ERR_TIMEOUT, GH_ERR_CUDA, GH_ERR_STATE = range(6)
+
+_VP = ctypes.c_void_p
+_I = ctypes.c_int
+_LL = ctypes.c_longlong
+_SIGS = {
+    "gh_status_string": (ctypes.c_char_p, [_I]),
+    "gh_heap_create": (_I, [ctypes.POINTER(_VP), _I, _I, _I, _I, _I, _VP]),
+    "gh_heap_destroy": (_I, [_VP]),
+    "gh_heap_reset": (_I, [_VP, _VP]),
+    "gh_heap_set_timeout": (_I, [_VP, ctypes.c_double]),
+    "gh_heap_set_block_threads": (_I, [_VP, _I]),
+    "gh_heap_set_grid": (_I, [_VP, _I]),
+    "gh_heap_insert": (_I, [_VP, _VP, _LL, _I, _VP]),
+    "gh_heap_delete": (_I, [_VP, _VP, _LL, ctypes.POINTER(_LL), _VP]),
+    "gh_heap_sync": (_I, [_VP, _VP]),
+    "gh_heap_insert_batch": (_I, [_VP, _VP, _I, _VP]),
+    "gh_heap_delete_batch": (_I, [_VP, _VP, ctypes.POINTER(_I), _VP]),
+    "gh_heap_sort": (_I, [_VP, _VP, _LL, _VP, _VP]),
+    "gh_heap_check": (_I, [_VP, ctypes.POINTER(_I), ctypes.c_char_p, _I, _VP]),
+    "gh_heap_item_count": (_I, [_VP, ctypes.POINTER(_LL)]),
+    "gh_heap_node_count": (_I, [_VP, ctypes.POINTER(_I)]),
+    "gh_heap_is_empty": (_I, [_VP, ctypes.POINTER(_I)]),
+    "gh_heap_snapshot": (_I, [_VP, _VP, _VP, _VP]),
+    "gh_heap_inject_lock": (_I, [_VP, _I, _I]),
+    "gh_heap_view_bytes": (ctypes.c_size_t, []),
+    "gh_heap_device_view": (_I, [_VP, _VP, ctypes.c_size_t]),
+    "gh_heap_smem_bytes": (ctypes.c_size_t, [_I, _I]),
+    "gh_heap_info": (_I, [_VP] + [ctypes.POINTER(_I)] * 7),
+}
+
+_lib = None
+
+
+def build(verbose=False):
+    """Compiles the CUDA library in-tree (gpuheap_gb300/builder.py)."""
+    from . import builder
+    return builder.build(verbose=verbose)
+
+
+def lib():
+    """The loaded C ABI library; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(library_path):
+            raise RuntimeError(
+                f"gpuheap_gb300: {library_path} is missing; build it with "
+                "`python -c 'import gpuheap_gb300 as g; g.build()'`")
+        so = ctypes.CDLL(library_path)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(so, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = so
+    return _lib
+
+
+class HeapError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        msg = lib().gh_status_string(status).decode()
+        super().__init__(f"{where}: {msg} (status {status})")
+
+
+def _check(status, where):
+    if status != GH_OK:
+        raise HeapError(status, where)
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    return t.data_ptr()
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return s.cuda_stream
+
+
+class Heap:
+    """One batched min-heap on the current CUDA device.
+
+    Heap(batch_num, batch_size, init_limits) as in the reference
+    (heap/tditdd/heap.cuh:33-67): batch_num full nodes of batch_size sorted
+    keys plus the partial buffer (node 0).  Every key must be strictly below
+    init_limits (default: the key type's maximum).
+    """
+
+    def __init__(self, batch_num, batch_size, init_limits=None, *, key="u32", variant="bottomup",
+                 partial_buffer=True):
+        if key not in KEY_KINDS:
+            raise ValueError(f"key must be one of {sorted(KEY_KINDS)}")
+        if variant not in _VARIANTS:
+            raise ValueError(f"variant must be one of {sorted(_VARIANTS)}")
+        self.key = key
+        self.variant = "topdown" if _VARIANTS[variant] == 0 else "bottomup"
+        self.partial_buffer = bool(partial_buffer)
+        self.batch_num = int(batch_num)
+        self.batch_size = int(batch_size)
+        self.key_bytes = _KEY_BYTES[key]
+        self._h = _VP()
+        lim = None
+        if init_limits is not None:
+            lim = _KEY_CTYPE[key](init_limits)
+        _check(lib().gh_heap_create(ctypes.byref(self._h), KEY_KINDS[key], _VARIANTS[variant],
+                                    1 if partial_buffer else 0, self.batch_num, self.batch_size,
+                                    ctypes.byref(lim) if lim is not None else None), "Heap()")
+        if init_limits is None:
+            init_limits = {"u32": 2**32 - 1, "i32": 2**31 - 1, "u64": 2**64 - 1}[key]
+        self.init_limits = int(init_limits)
+
+    # ---------------------------------------------------------------- lifetime
+    def close(self):
+        if self._h:
+            lib().gh_heap_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def reset(self, stream=None):
+        """reset(): heap/tditdd/heap.cuh:69-91."""
+        _check(lib().gh_heap_reset(self._h, _stream(stream)), "reset")
+        _check(lib().gh_heap_sync(self._h, _stream(stream)), "reset")
+
+    # ---------------------------------------------------------------- tuning
+    def set_timeout(self, seconds):
+        _check(lib().gh_heap_set_timeout(self._h, float(seconds)), "set_timeout")
+
+    def set_block_threads(self, threads):
+        _check(lib().gh_heap_set_block_threads(self._h, int(threads)), "set_block_threads")
+
+    def set_grid(self, blocks):
+        _check(lib().gh_heap_set_grid(self._h, int(blocks)), "set_grid")
+
+    def info(self):
+        vals = [_I() for _ in range(7)]
+        _check(lib().gh_heap_info(self._h, *[ctypes.byref(v) for v in vals]), "info")
+        names = ["key_kind", "variant", "partial_buffer", "batch_num", "batch_size", "block_threads", "grid"]
+        return {n: v.value for n, v in zip(names, vals)}
+
+    # ---------------------------------------------------------------- operations
+    def insertion(self, items, size, stream=None):
+        """One Heap::insertion(items, size) by one block (heap/tditdd/heap.cuh:536)."""
+        _check(lib().gh_heap_insert_batch(self._h, _ptr(items), int(size), _stream(stream)), "insertion")
+
+    def delete_root(self, items, stream=None):
+        """One deleteRoot (+ deleteUpdate) by one block; HEAP_SORT output at
+        items + the heap's output cursor.  Returns the number of keys written."""
+        sz = _I()
+        _check(lib().gh_heap_delete_batch(self._h, _ptr(items), ctypes.byref(sz), _stream(stream)), "deleteRoot")
+        return sz.value
+
+    def insert(self, keys, n=None, chunk=0, stream=None):
+        """Bulk insertion of n keys in insertion() calls of `chunk` keys over
+        the heap's grid (insertKernel, test/heap_test.cu:44-58).  Asynchronous."""
+        n = keys.numel() if n is None else int(n)
+        _check(lib().gh_heap_insert(self._h, _ptr(keys), n, int(chunk), _stream(stream)), "insert")
+
+    def delete(self, out, max_keys=None, stream=None, sync=True):
+        """Deletes until empty (deleteKernel, test/heap_test.cu:60-77) into
+        out[0, n) in ascending order; returns n (None when sync=False)."""
+        max_keys = out.numel() if max_keys is None else int(max_keys)
+        if not sync:
+            _check(lib().gh_heap_delete(self._h, _ptr(out), max_keys, None, _stream(stream)), "delete")
+            return None
+        got = _LL()
+        _check(lib().gh_heap_delete(self._h, _ptr(out), max_keys, ctypes.byref(got), _stream(stream)), "delete")
+        return got.value
+
+    def sort(self, keys, out, n=None, stream=None):
+        """Heap-sort: reset, insert all keys, delete all (test/partial_heap_test.cu:88-176)."""
+        n = keys.numel() if n is None else int(n)
+        _check(lib().gh_heap_sort(self._h, _ptr(keys), n, _ptr(out), _stream(stream)), "sort")
+
+    def sync(self, stream=None):
+        _check(lib().gh_heap_sync(self._h, _stream(stream)), "sync")
+
+    # ---------------------------------------------------------------- inspection
+    def check_insert_heap(self, stream=None):
+        """checkInsertHeap() on the device; returns (ok, message)."""
+        ok = _I()
+        msg = ctypes.create_string_buffer(256)
+        _check(lib().gh_heap_check(self._h, ctypes.byref(ok), msg, 256, _stream(stream)), "checkInsertHeap")
+        return bool(ok.value), msg.value.decode()
+
+    def checkInsertHeap(self):
+        return self.check_insert_heap()[0]
+
+    def item_count(self):
+        n = _LL()
+        _check(lib().gh_heap_item_count(self._h, ctypes.byref(n)), "itemCount")
+        return n.value
+
+    def node_count(self):
+        n = _I()
+        _check(lib().gh_heap_node_count(self._h, ctypes.byref(n)), "nodeCount")
+        return n.value
+
+    def is_empty(self):
+        e = _I()
+        _check(lib().gh_heap_is_empty(self._h, ctypes.byref(e)), "isEmpty")
+        return bool(e.value)
+
+    itemCount = item_count
+    nodeCount = node_count
+    isEmpty = is_empty
+
+    def snapshot(self):
+        """(items, status, counters) as numpy arrays; counters =
+        [batchCount, partialBufferSize, deleteCount, err, errOp, errNode, errState]."""
+        import numpy as np
+        dt = {"u32": np.uint32, "i32": np.int32, "u64": np.uint64}[self.key]
+        items = np.empty((self.batch_num + 1) * self.batch_size, dt)
+        status = np.empty(self.batch_num + 1, np.int32)
+        counters = np.zeros(7, np.int32)
+        _check(lib().gh_heap_snapshot(self._h, items.ctypes.data, status.ctypes.data, counters.ctypes.data),
+               "snapshot")
+        return items, status, counters
+
+    def inject_lock(self, node, state):
+        """Fault injection: leave node's lock word in `state` (tests of the bounded waits)."""
+        _check(lib().gh_heap_inject_lock(self._h, int(node), int(state)), "inject_lock")
+
+    def device_view(self):
+        """Bytes of the gh::Heap<K, variant, partial_buffer> device view."""
+        n = lib().gh_heap_view_bytes()
+        buf = ctypes.create_string_buffer(n)
+        _check(lib().gh_heap_device_view(self._h, buf, n), "device_view")
+        return buf.raw
+
+    @staticmethod
+    def smem_bytes(key, batch_size):
+        return lib().gh_heap_smem_bytes(KEY_KINDS[key], int(batch_size))

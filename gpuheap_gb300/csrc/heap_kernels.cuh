@@ -1,0 +1,148 @@
+// Kernels behind the C ABI: bulk insert/delete drivers (the reference's
+// insertKernel/deleteKernel of test/heap_test.cu:13-77), single-operation
+// launches, device-side checkInsertHeap and state initialisation.
+#pragma once
+#include <climits>
+#include <cstdint>
+
+#include "gpuheap_device.cuh"
+
+namespace gh {
+namespace impl {
+
+// Everything the host keeps about one heap, independent of the key type.
+struct Desc {
+    void* items;
+    int* status;
+    HeapState* state;
+    uint64_t initBits;  // init_limits, in the low bytes
+    int batchNum;
+    int batchSize;
+    long long timeoutNs;
+    int variant;
+    int pb;
+    int keyBytes;
+};
+
+// insertKernel: chunks of `chunk` keys, grid-strided over blocks.
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_insert(H h, const K* __restrict__ keys, long long n, int chunk) {
+    const long long nchunks = (n + chunk - 1) / chunk;
+    for (long long i = blockIdx.x; i < nchunks; i += gridDim.x) {
+        const long long off = i * chunk;
+        const long long rem = n - off;
+        const int size = rem < chunk ? static_cast<int>(rem) : chunk;
+        h.insertion(keys + off, size, 0);
+        if (h.failed()) return;
+    }
+}
+
+// deleteKernel: every block deletes until the heap is empty (or the output
+// limit / an error stops deleteRoot).
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_delete(H h, K* out) {
+    for (;;) {
+        int size = 0;
+        const bool more = h.deleteRoot(out, size);
+        if (more) h.deleteUpdate(0);
+        if (size == 0) return;
+    }
+}
+
+// One deleteRoot (+ deleteUpdate) by one block; the size goes to *sizeOut.
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_delete_one(H h, K* out, int* sizeOut) {
+    int size = 0;
+    const bool more = h.deleteRoot(out, size);
+    if (more) h.deleteUpdate(0);
+    if (threadIdx.x == 0) *sizeOut = size;
+}
+
+template <typename K>
+__global__ void k_fill(K* p, size_t n, K v) {
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = v;
+}
+
+static __global__ void k_init_state(HeapState* st, int deleteCount) {
+    if (threadIdx.x == 0) {
+        st->batchCount = 0;
+        st->partialBufferSize = 0;
+        st->deleteCount = deleteCount;
+        st->outLimit = INT_MAX;
+        st->err = 0;
+        st->errOp = 0;
+        st->errNode = 0;
+        st->errState = 0;
+    }
+}
+
+// Sets the HEAP_SORT cursor (unless deleteCount < 0) and the output limit.
+static __global__ void k_set_output(HeapState* st, int deleteCount, int outLimit) {
+    if (threadIdx.x == 0) {
+        if (deleteCount >= 0) st->deleteCount = deleteCount;
+        st->outLimit = outLimit;
+    }
+}
+
+// Result of the device-side heap check.
+struct CheckResult {
+    int badNode;  // smallest failing node (INT_MAX when none)
+    int code;     // what failed at badNode (see k_check)
+    int detail;
+    int pad;
+};
+
+__device__ __forceinline__ int rev_idx(int i) {
+    if (i <= 1) return i;
+    const int l = __clz(i) + 1;
+    return static_cast<int>((__brev(static_cast<unsigned>(i)) >> l) | (1u << (32 - l)));
+}
+
+// checkInsertHeap on the device (heap/tditdd/heap.cuh:123-176,
+// heap/buitdd/heap.cuh:118-172): one warp per node.  Codes: 1 status not
+// AVAIL, 2 node unsorted, 3 node starts below its parent's end, 4 partial
+// buffer unsorted, 5 partial buffer below the root, 6 partial buffer lock.
+template <typename K>
+__global__ void k_check(const K* __restrict__ items, const int* __restrict__ status, const HeapState* st,
+                        int variant, int B, CheckResult* res) {
+    const int bc = st->batchCount, ps = st->partialBufferSize;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    auto report = [&](int node, int code, int detail) {
+        const int old = atomicMin(&res->badNode, node);
+        if (old > node) { res->code = code; res->detail = detail; }
+    };
+    if (warp == 0) {
+        if (lane == 0 && status[0] != 0) report(0, 6, status[0]);
+        if (bc != 0 && ps != 0) {
+            if (lane == 0 && items[2 * B - 1] > items[0]) report(0, 5, 0);
+            for (int j = 1 + lane; j < ps; j += 32)
+                if (items[j] < items[j - 1]) { report(0, 4, j); break; }
+        }
+    }
+    for (int i = 1 + warp; i <= bc; i += nwarps) {
+        const K* nd = items + static_cast<size_t>(i) * B;
+        if (lane == 0) {
+            if (status[i] != 0) report(i, 1, status[i]);
+            if (i > 1) {
+                const int p = variant == kTopDown ? i / 2 : rev_idx(rev_idx(i) >> 1);
+                if (nd[0] < items[static_cast<size_t>(p) * B + B - 1]) report(i, 3, p);
+            }
+        }
+        bool bad = false;
+        int where = 0;
+        for (int j = 1 + lane; j < B; j += 32)
+            if (nd[j] < nd[j - 1]) { bad = true; where = j; break; }
+        const unsigned m = __ballot_sync(0xffffffffu, bad);
+        if (m) {
+            const int src = __ffs(m) - 1;
+            where = __shfl_sync(0xffffffffu, where, src);
+            if (lane == 0) report(i, 2, where);
+        }
+    }
+}
+
+}  // namespace impl
+}  // namespace gh

@@ -1,0 +1,136 @@
+// Launchers for the heap kernels, instantiated once per key type in
+// heap_inst_{u32,i32,u64}.cu so the three instantiation sets compile in
+// parallel.  The merge width IPT = 2 * batchSize / threads is a template
+// parameter of every kernel (1, 2, 4 or 8 keys per thread per merge).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "heap_kernels.cuh"
+
+namespace gh {
+namespace impl {
+
+struct LaunchArgs {
+    const Desc* d;
+    int threads;
+    int grid;
+    cudaStream_t stream;
+    int* opSize;
+};
+
+template <typename K>
+cudaError_t launch_insert(const LaunchArgs& a, const K* keys, long long n, int chunk);
+template <typename K>
+cudaError_t launch_erase(const LaunchArgs& a, K* out);
+template <typename K>
+cudaError_t launch_erase_one(const LaunchArgs& a, K* out);
+// Bytes of gh::Heap<K, variant, pb> (IPT chosen at run time) for application kernels.
+template <typename K>
+void device_view(const Desc& d, void* out, size_t* bytes);
+
+#ifdef GH_INSTANTIATE
+template <typename H>
+inline cudaError_t allow_smem(const void* fn, size_t smem) {
+    if (smem <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+}
+
+// Calls f(Heap<K, V, PB, IPT>{}) for the run-time variant, pb flag and IPT.
+template <typename K, typename F>
+inline cudaError_t dispatch(const Desc& d, int threads, F&& f) {
+    const int ipt = 2 * d.batchSize / threads;
+    auto by_ipt = [&](auto v, auto pb) -> cudaError_t {
+        constexpr int V = decltype(v)::value;
+        constexpr bool PB = decltype(pb)::value;
+        switch (ipt) {
+            case 1: return f(Heap<K, V, PB, 1>{});
+            case 2: return f(Heap<K, V, PB, 2>{});
+            case 4: return f(Heap<K, V, PB, 4>{});
+            case 8: return f(Heap<K, V, PB, 8>{});
+            default: return cudaErrorInvalidValue;
+        }
+    };
+    using TDv = std::integral_constant<int, kTopDown>;
+    using BUv = std::integral_constant<int, kBottomUp>;
+    using Yes = std::integral_constant<bool, true>;
+    using No = std::integral_constant<bool, false>;
+    if (d.variant == kTopDown) return d.pb ? by_ipt(TDv{}, Yes{}) : by_ipt(TDv{}, No{});
+    return d.pb ? by_ipt(BUv{}, Yes{}) : by_ipt(BUv{}, No{});
+}
+
+template <typename H>
+inline H view_of(const Desc& d, int sortOutput) {
+    H h;
+    h.heapItems = static_cast<typename H::key_type*>(d.items);
+    h.status = d.status;
+    h.state = d.state;
+    __builtin_memcpy(&h.init_limits, &d.initBits, sizeof(typename H::key_type));
+    h.batchNum = d.batchNum;
+    h.batchSize = d.batchSize;
+    h.sortOutput = sortOutput;
+    h.timeoutNs = d.timeoutNs;
+    return h;
+}
+
+template <typename K>
+cudaError_t launch_insert(const LaunchArgs& a, const K* keys, long long n, int chunk) {
+    return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
+        using H = decltype(proto);
+        const H h = view_of<H>(*a.d, 1);
+        const size_t smem = H::smemBytes(a.d->batchSize);
+        cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_insert<H, K>), smem);
+        if (e != cudaSuccess) return e;
+        const long long nchunks = (n + chunk - 1) / chunk;
+        const int g = static_cast<int>(nchunks < a.grid ? nchunks : a.grid);
+        k_insert<H, K><<<g, a.threads, smem, a.stream>>>(h, keys, n, chunk);
+        return cudaGetLastError();
+    });
+}
+
+template <typename K>
+cudaError_t launch_erase(const LaunchArgs& a, K* out) {
+    return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
+        using H = decltype(proto);
+        const H h = view_of<H>(*a.d, 1);
+        const size_t smem = H::smemBytes(a.d->batchSize);
+        cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_delete<H, K>), smem);
+        if (e != cudaSuccess) return e;
+        k_delete<H, K><<<a.grid, a.threads, smem, a.stream>>>(h, out);
+        return cudaGetLastError();
+    });
+}
+
+template <typename K>
+cudaError_t launch_erase_one(const LaunchArgs& a, K* out) {
+    return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
+        using H = decltype(proto);
+        const H h = view_of<H>(*a.d, 1);
+        const size_t smem = H::smemBytes(a.d->batchSize);
+        cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_delete_one<H, K>), smem);
+        if (e != cudaSuccess) return e;
+        k_delete_one<H, K><<<1, a.threads, smem, a.stream>>>(h, out, a.opSize);
+        return cudaGetLastError();
+    });
+}
+
+template <typename K>
+void device_view(const Desc& d, void* out, size_t* bytes) {
+    auto put = [&](auto proto) {
+        using H = decltype(proto);
+        const H h = view_of<H>(d, 0);
+        __builtin_memcpy(out, &h, sizeof(H));
+        *bytes = sizeof(H);
+    };
+    if (d.variant == kTopDown) { if (d.pb) put(Heap<K, kTopDown, true>{}); else put(Heap<K, kTopDown, false>{}); }
+    else { if (d.pb) put(Heap<K, kBottomUp, true>{}); else put(Heap<K, kBottomUp, false>{}); }
+}
+
+#define GH_INSTANTIATE_KEY(K)                                                                    \
+    template cudaError_t launch_insert<K>(const LaunchArgs&, const K*, long long, int);          \
+    template cudaError_t launch_erase<K>(const LaunchArgs&, K*);                                 \
+    template cudaError_t launch_erase_one<K>(const LaunchArgs&, K*);                             \
+    template void device_view<K>(const Desc&, void*, size_t*);
+#endif  // GH_INSTANTIATE
+
+}  // namespace impl
+}  // namespace gh

@@ -1,0 +1,132 @@
+/* gpuheap.h -- C ABI of the GB300 batched priority queue (BGPQ).
+ *
+ * Plain pointers and sizes only.  Device buffers are raw device pointers;
+ * `stream` is a cudaStream_t passed as void* (NULL = the legacy default
+ * stream).  Every entry point returns a gh_status.
+ *
+ * The reference (ruadapt/gpuheap) has no FFI: its interface is the C++ class
+ * template Heap<K> in heap/{tditdd,tditdd_np,buitdd,buitdd_np}/heap.cuh, whose
+ * variant is chosen by include path.  Each entry point below names the member
+ * or test-driver code it replaces; the variant, partial-buffer flag and key
+ * type become run-time arguments here.  Device code keeps the reference's
+ * member-function shape through include/gpuheap_device.cuh.
+ */
+#ifndef GPUHEAP_H
+#define GPUHEAP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GH_OK = 0,
+    GH_ERR_INVALID = 1,   /* bad argument (size, alignment, variant ...) */
+    GH_ERR_CAPACITY = 2,  /* insertion found no free node (batch_num reached) */
+    GH_ERR_TIMEOUT = 3,   /* a device-side wait passed the heap's time limit */
+    GH_ERR_CUDA = 4,      /* a CUDA runtime call failed */
+    GH_ERR_STATE = 5      /* the heap recorded an earlier device error; reset it */
+} gh_status;
+
+typedef enum { GH_KEY_U32 = 0, GH_KEY_I32 = 1, GH_KEY_U64 = 2 } gh_key_kind;
+typedef enum { GH_TOPDOWN = 0, GH_BOTTOMUP = 1 } gh_variant;
+
+typedef struct gh_heap gh_heap;
+
+const char* gh_status_string(gh_status s);
+
+/* Heap<K>(batch_num, batch_size, init_limits): heap/tditdd/heap.cuh:33-67,
+ * heap/buitdd/heap.cuh:34-68; variant = include path (test/Makefile:10-20).
+ * batch_size: power of two in [16, 4096].  init_limits points to one key of
+ * the chosen kind (NULL = the kind's maximum); every real key must be
+ * strictly below it.  Nodes are filled with init_limits on the device. */
+gh_status gh_heap_create(gh_heap** out, int key_kind, int variant, int partial_buffer, int batch_num,
+                         int batch_size, const void* init_limits);
+/* ~Heap(): heap/tditdd/heap.cuh:93-116. */
+gh_status gh_heap_destroy(gh_heap* h);
+/* reset(): heap/tditdd/heap.cuh:69-91 (also clears a recorded device error). */
+gh_status gh_heap_reset(gh_heap* h, void* stream);
+
+/* Time limit of every device-side wait (default 2 s). */
+gh_status gh_heap_set_timeout(gh_heap* h, double seconds);
+/* Threads per block for the bulk entry points (0 = automatic: 16-byte merge
+ * runs per thread); a power of two in [32, 1024] with 2*batch_size/threads
+ * in {1, 2, 4, 8}. */
+gh_status gh_heap_set_block_threads(gh_heap* h, int threads);
+/* Blocks for the bulk entry points (0 = one per SM). */
+gh_status gh_heap_set_grid(gh_heap* h, int blocks);
+
+/* insertKernel (test/heap_test.cu:44-58, artifacts/synthetic/sort.cu:32-46):
+ * inserts keys_dev[0, n) in insertion() calls of `chunk` keys (0 = batch_size;
+ * chunk <= batch_size), spread over the heap's grid. */
+gh_status gh_heap_insert(gh_heap* h, const void* keys_dev, long long n, int chunk, void* stream);
+
+/* deleteKernel (test/heap_test.cu:60-77): deleteRoot/deleteUpdate until the
+ * heap is empty or the next deleted batch would not fit in max_keys.  Keys
+ * are written in ascending order (HEAP_SORT) to out_dev[0, *n_out).  When
+ * n_out is not NULL the call synchronizes the stream to read the count. */
+gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long long* n_out, void* stream);
+
+/* Waits for the stream and reports the first error the heap recorded on the
+ * device (the bulk entry points above return before their kernels finish). */
+gh_status gh_heap_sync(gh_heap* h, void* stream);
+
+/* One Heap::insertion(items, size, 0) by one thread block
+ * (heap/tditdd/heap.cuh:536, heap/buitdd/heap.cuh:484); 0 < size <= batch_size
+ * (size 0 is a no-op). */
+gh_status gh_heap_insert_batch(gh_heap* h, const void* keys_dev, int size, void* stream);
+/* One Heap::deleteRoot(items, size) (+ deleteUpdate when it returns true) by
+ * one thread block (heap/tditdd/heap.cuh:267-534).  HEAP_SORT semantics: the
+ * keys land at out_dev + (the heap's output cursor), the cursor advances, and
+ * gh_heap_reset sets it back to 0.  Synchronizes the stream; *size = keys written. */
+gh_status gh_heap_delete_batch(gh_heap* h, void* out_dev, int* size, void* stream);
+
+/* The plain heap-sort (test/partial_heap_test.cu:88-176, without the
+ * concurrent phase): reset, insert in_dev[0, n) in batch_size calls, then
+ * delete everything into out_dev[0, n).  out_dev must hold n keys. */
+gh_status gh_heap_sort(gh_heap* h, const void* in_dev, long long n, void* out_dev, void* stream);
+
+/* checkInsertHeap(): heap/tditdd/heap.cuh:123-176, heap/buitdd/heap.cuh:118-172,
+ * run on the device over the whole heap.  *ok = 1 when valid; otherwise msg
+ * (if not NULL) describes the first violation.  Synchronizes the stream. */
+gh_status gh_heap_check(gh_heap* h, int* ok, char* msg, int msg_len, void* stream);
+
+/* itemCount() / nodeCount() / isEmpty(): heap/tditdd/heap.cuh:217-235. */
+gh_status gh_heap_item_count(gh_heap* h, long long* n);
+gh_status gh_heap_node_count(gh_heap* h, int* n);
+gh_status gh_heap_is_empty(gh_heap* h, int* empty);
+
+/* Host copy of the heap's memory (printHeap, heap/tditdd/heap.cuh:179-208):
+ * items_host gets (batch_num + 1) * batch_size keys, status_host
+ * batch_num + 1 lock words, counters_host {batchCount, partialBufferSize,
+ * deleteCount, err, errOp, errNode, errState}.  Any pointer may be NULL. */
+gh_status gh_heap_snapshot(gh_heap* h, void* items_host, int* status_host, int* counters_host);
+
+/* Fault injection from the host, for tests of the bounded waits: writes
+ * `state` into the lock word of `node` (synchronously).  A lock word left
+ * taken makes the next operation that needs it wait out the heap's time
+ * limit and report GH_ERR_TIMEOUT; gh_heap_reset clears it.  The reference
+ * has no counterpart (its waits are unbounded, heap/tditdd/heap.cuh:250). */
+gh_status gh_heap_inject_lock(gh_heap* h, int node, int state);
+
+/* The device view for application kernels: writes the bytes of a
+ * gh::Heap<K, variant, partial_buffer> (include/gpuheap_device.cuh) to
+ * view_out (view_bytes must be >= gh_heap_view_bytes()).  Replaces the
+ * shallow copy of the host object to the device (test/heap_test.cu:121-129). */
+size_t gh_heap_view_bytes(void);
+gh_status gh_heap_device_view(gh_heap* h, void* view_out, size_t view_bytes);
+
+/* Dynamic shared memory one block needs for the heap's operations
+ * (heap/tditdd/heap.cuh: 3 * batch_size keys of merge space, plus control). */
+size_t gh_heap_smem_bytes(int key_kind, int batch_size);
+
+/* Properties. */
+gh_status gh_heap_info(gh_heap* h, int* key_kind, int* variant, int* partial_buffer, int* batch_num,
+                       int* batch_size, int* block_threads, int* grid);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,87 @@
+/* CPU oracle for the batched priority queue (BGPQ) hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: only tests, the smoke check and the CPU leg of the
+ * benchmark load this library.  It is the checker, never the thing measured
+ * or shipped; the product path (gpuheap_gb300) never calls it.
+ *
+ * Parity is pinned: tests/golden/ holds vectors produced by the reference's
+ * own heap headers run sequentially on the host (oracle/ref_driver.cpp +
+ * oracle/ref_shim.h), and the CPU tests replay them through this restatement
+ * bit-exactly.
+ *
+ * Contents
+ *   - counter-based seeded key generators (splitmix64 finaliser, Steele et al.
+ *     2014) for the four key distributions of the plain heap-sort workload;
+ *   - std::sort, single- and multi-threaded (the reference's own test oracle:
+ *     test/heap_test.cu:118 and :163-170);
+ *   - checkInsertHeap for both node layouts (heap/tditdd/heap.cuh:123-176,
+ *     heap/buitdd/heap.cuh:118-172);
+ *   - a sequential model of Heap<K>::insertion / deleteRoot / deleteUpdate for
+ *     the four variants (heap/{tditdd,tditdd_np,buitdd,buitdd_np}/heap.cuh).
+ *     With one thread block the GPU heap is deterministic, and because the keys
+ *     are plain integers every merge has a unique result, so the GPU's node
+ *     contents must equal this model's bit for bit.
+ */
+#ifndef GPUHEAP_ORACLE_H
+#define GPUHEAP_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* distributions */
+enum { GHO_UNIFORM = 0, GHO_SORTED = 1, GHO_REVERSE = 2, GHO_ZIPF = 3 };
+
+/* u32 keys in [0, 2^32-2] (UINT32_MAX is reserved as init_limits). */
+void gho_gen_u32(uint64_t seed, int dist, uint64_t n, uint32_t* out, int threads);
+/* u64 keys = (u32 key << 32) | input index. */
+void gho_gen_u64(uint64_t seed, int dist, uint64_t n, uint64_t* out, int threads);
+/* i32 keys in [INT32_MIN, INT32_MAX-1]. */
+void gho_gen_i32(uint64_t seed, int dist, uint64_t n, int32_t* out, int threads);
+
+void gho_sort_u32(uint32_t* a, uint64_t n, int threads);
+void gho_sort_u64(uint64_t* a, uint64_t n, int threads);
+void gho_sort_i32(int32_t* a, uint64_t n, int threads);
+
+/* Bit-reversal of the bits below the leading one (heap/buitdd/heap.cuh:238-255). */
+uint32_t gho_reversed_idx(uint32_t i);
+
+/* checkInsertHeap over a host copy.  variant: 0 top-down, 1 bottom-up.
+ * status may be NULL (then the state checks are skipped).  Returns 1 when the
+ * heap is valid, 0 otherwise with a reason in msg. */
+int gho_check_u32(int variant, const uint32_t* items, const int* status, int batch_size,
+                  int batch_count, int partial_size, char* msg, int msg_len);
+int gho_check_u64(int variant, const uint64_t* items, const int* status, int batch_size,
+                  int batch_count, int partial_size, char* msg, int msg_len);
+int gho_check_i32(int variant, const int32_t* items, const int* status, int batch_size,
+                  int batch_count, int partial_size, char* msg, int msg_len);
+
+/* Sequential model.  variant: 0 top-down, 1 bottom-up; pb: partial buffer. */
+void* gho_model_create_u32(int variant, int pb, int batch_num, int batch_size, uint32_t init_limits);
+void* gho_model_create_u64(int variant, int pb, int batch_num, int batch_size, uint64_t init_limits);
+void* gho_model_create_i32(int variant, int pb, int batch_num, int batch_size, int32_t init_limits);
+/* One insertion(items, size) call, size <= batch_size.  Returns 0, or -2 when
+ * the heap has no free node. */
+int gho_model_insert_u32(void* m, const uint32_t* items, int size);
+int gho_model_insert_u64(void* m, const uint64_t* items, int size);
+int gho_model_insert_i32(void* m, const int32_t* items, int size);
+/* deleteRoot (+ deleteUpdate) with HEAP_SORT output at out + deleteCount.
+ * Returns the number of keys written (0 when empty). */
+int gho_model_delete_u32(void* m, uint32_t* out);
+int gho_model_delete_u64(void* m, uint64_t* out);
+int gho_model_delete_i32(void* m, int32_t* out);
+/* Copies (batch_num + 1) * batch_size keys and {batchCount, partialBufferSize, deleteCount}. */
+void gho_model_state_u32(void* m, uint32_t* items, int* counters);
+void gho_model_state_u64(void* m, uint64_t* items, int* counters);
+void gho_model_state_i32(void* m, int32_t* items, int* counters);
+void gho_model_destroy(void* m);
+
+/* Closed-form algorithmic byte count of one heap-sort (bytes moved by the
+ * BGPQ node traffic, independent of the implementation). */
+double gho_sort_bytes(uint64_t n, int batch_size, int key_bytes, int partial_buffer);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,125 @@
+"""ctypes access to the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+CPU leg of bench.py, as the checker -- never by the product path.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+DISTS = {"uniform": 0, "sorted": 1, "reverse": 2, "zipf": 3}
+DTYPES = {"u32": np.uint32, "u64": np.uint64, "i32": np.int32}
+CTYPES = {"u32": ctypes.c_uint32, "u64": ctypes.c_uint64, "i32": ctypes.c_int32}
+INIT = {"u32": 2**32 - 1, "u64": 2**64 - 1, "i32": 2**31 - 1}
+_VP = ctypes.c_void_p
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        src = [os.path.join(HERE, f) for f in ("bgpq_oracle.cpp", "bgpq_oracle.h")]
+        if not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in src):
+            subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+        so = ctypes.CDLL(LIB)
+        for k in DTYPES:
+            getattr(so, f"gho_gen_{k}").argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_uint64, _VP, ctypes.c_int]
+            getattr(so, f"gho_sort_{k}").argtypes = [_VP, ctypes.c_uint64, ctypes.c_int]
+            getattr(so, f"gho_check_{k}").argtypes = [ctypes.c_int, _VP, _VP, ctypes.c_int, ctypes.c_int,
+                                                     ctypes.c_int, ctypes.c_char_p, ctypes.c_int]
+            f = getattr(so, f"gho_model_create_{k}")
+            f.restype = _VP
+            f.argtypes = [ctypes.c_int] * 4 + [CTYPES[k]]
+            getattr(so, f"gho_model_insert_{k}").argtypes = [_VP, _VP, ctypes.c_int]
+            getattr(so, f"gho_model_delete_{k}").argtypes = [_VP, _VP]
+            getattr(so, f"gho_model_state_{k}").argtypes = [_VP, _VP, _VP]
+        so.gho_model_destroy.argtypes = [_VP]
+        so.gho_reversed_idx.restype = ctypes.c_uint32
+        so.gho_reversed_idx.argtypes = [ctypes.c_uint32]
+        so.gho_sort_bytes.restype = ctypes.c_double
+        so.gho_sort_bytes.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        _lib = so
+    return _lib
+
+
+def gen(key, seed, dist, n, threads=None):
+    """Seeded keys of the plain heap-sort workload (see bgpq_oracle.h)."""
+    out = np.empty(n, DTYPES[key])
+    th = threads or os.cpu_count() or 1
+    getattr(lib(), f"gho_gen_{key}")(seed, DISTS[dist], n, out.ctypes.data, th)
+    return out
+
+
+def sort(a, threads=1):
+    """std::sort (threads > 1: per-thread std::sort + pairwise std::merge), in place."""
+    key = {np.dtype(np.uint32): "u32", np.dtype(np.uint64): "u64", np.dtype(np.int32): "i32"}[a.dtype]
+    assert a.flags.c_contiguous
+    getattr(lib(), f"gho_sort_{key}")(a.ctypes.data, a.size, threads)
+    return a
+
+
+def check_heap(variant, items, status, batch_size, batch_count, partial_size):
+    """checkInsertHeap restated; returns (ok, message)."""
+    key = {np.dtype(np.uint32): "u32", np.dtype(np.uint64): "u64", np.dtype(np.int32): "i32"}[items.dtype]
+    msg = ctypes.create_string_buffer(200)
+    v = 0 if variant in ("topdown", "td", 0) else 1
+    st = None if status is None else np.ascontiguousarray(status, np.int32)
+    ok = getattr(lib(), f"gho_check_{key}")(v, items.ctypes.data, None if st is None else st.ctypes.data,
+                                            int(batch_size), int(batch_count), int(partial_size), msg, 200)
+    return Result(bool(ok), msg.value.decode())
+
+
+class Result(tuple):
+    def __new__(cls, ok, msg):
+        return tuple.__new__(cls, (ok, msg))
+
+    def __bool__(self):
+        return self[0]
+
+
+def reversed_idx(i):
+    return lib().gho_reversed_idx(i)
+
+
+def sort_bytes(n, batch_size, key_bytes, partial_buffer):
+    """Algorithmic node traffic of one heap-sort in bytes."""
+    return lib().gho_sort_bytes(n, batch_size, key_bytes, 1 if partial_buffer else 0)
+
+
+class Model:
+    """Sequential Heap<K> model (insertion / deleteRoot+deleteUpdate)."""
+
+    def __init__(self, key, variant, partial_buffer, batch_num, batch_size, init_limits=None):
+        self.key = key
+        self.dt = DTYPES[key]
+        self.batch_num = batch_num
+        self.batch_size = batch_size
+        v = 0 if variant in ("topdown", "td", 0) else 1
+        lim = INIT[key] if init_limits is None else init_limits
+        self.h = getattr(lib(), f"gho_model_create_{key}")(v, 1 if partial_buffer else 0, batch_num, batch_size,
+                                                          CTYPES[key](lim))
+
+    def insert(self, items):
+        items = np.ascontiguousarray(items, self.dt)
+        return getattr(lib(), f"gho_model_insert_{self.key}")(self.h, items.ctypes.data, items.size)
+
+    def delete(self, out):
+        assert out.dtype == self.dt and out.flags.c_contiguous
+        return getattr(lib(), f"gho_model_delete_{self.key}")(self.h, out.ctypes.data)
+
+    def state(self):
+        items = np.empty((self.batch_num + 1) * self.batch_size, self.dt)
+        counters = np.zeros(3, np.int32)
+        getattr(lib(), f"gho_model_state_{self.key}")(self.h, items.ctypes.data, counters.ctypes.data)
+        return items, counters
+
+    def __del__(self):
+        try:
+            lib().gho_model_destroy(self.h)
+        except Exception:
+            pass

@@ -1,0 +1,171 @@
+"""Generate tests/golden/bgpq_ref_cases.npz from the reference's own heap code.
+
+Runs the reference's Heap<K> (heap/{tditdd,tditdd_np,buitdd,buitdd_np}/heap.cuh,
+compiled for the host by oracle/Makefile's `ref` target through
+oracle/ref_shim.h, one thread per "block") over seeded operation sequences and
+records, per case: the input keys, the operation list, every deleteRoot size,
+the HEAP_SORT output buffer, the heap memory and counters after the insert
+phase and at the end.  These vectors pin both the oracle restatement (CPU
+tests) and the CUDA path (GPU tests, one thread block, where the heap is
+deterministic).
+
+Usage (needs the reference tree; not run by the tests):
+    make -C oracle ref && python tests/golden/make_golden.py
+"""
+import ctypes
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+LIB = os.path.join(REPO, "oracle", "_ref", "libbgpq_ref.so")
+
+TYPES = {
+    "u32": (np.uint32, ctypes.c_uint32, 0xFFFFFFFF),
+    "u64": (np.uint64, ctypes.c_uint64, 2**64 - 1),
+    "i32": (np.int32, ctypes.c_int32, 2**31 - 1),
+}
+VARIANTS = ["tditdd", "tditdd_np", "buitdd", "buitdd_np"]
+VP = ctypes.c_void_p
+
+
+def keys_for(rng, kind, n, split):
+    """Seeded keys; with split=True the first half lies below the second half
+    (the shape of test/partial_heap_test.cu:114-119)."""
+    dt = TYPES[kind][0]
+    if kind == "u64":
+        lo, hi = 0, 2**63
+    elif kind == "i32":
+        lo, hi = -(2**31), 2**31 - 1
+    else:
+        lo, hi = 0, 2**32 - 1
+    if not split:
+        return rng.integers(lo, hi, n, dtype=dt)
+    mid = lo + (hi - lo) // 2
+    a = rng.integers(lo, mid, n // 2, dtype=dt)
+    b = rng.integers(mid, hi, n - n // 2, dtype=dt)
+    return np.concatenate([a, b])
+
+
+def make_ops(rng, scenario, np_variant, B, n):
+    """Operation list: a positive entry inserts that many keys, 0 deletes."""
+    ops = []
+    if scenario == "sort":
+        step = B if np_variant else B // 3
+        pos = 0
+        while pos < n:
+            s = min(step, n - pos)
+            ops.append(s)
+            pos += s
+        ops.append(-1)  # marks the end of the insert phase (snapshot)
+        ops += [0] * ((n + B - 1) // B + 1)
+    elif scenario == "concurrent":
+        half = n // 2
+        step = B if np_variant else B // 3
+        pos = 0
+        while pos < half:
+            s = min(step, half - pos)
+            ops.append(s)
+            pos += s
+        ops.append(-1)
+        step2 = B if np_variant else (2 * B) // 3
+        while pos < n:
+            s = min(step2, n - pos)
+            ops.append(s)
+            pos += s
+            ops.append(0)
+        ops += [0] * ((n + B - 1) // B + 2)
+    else:  # mixed
+        pos = 0
+        while pos < n:
+            if rng.random() < 0.65:
+                s = B if np_variant else int(rng.integers(1, B + 1))
+                s = min(s, n - pos)
+                ops.append(s)
+                pos += s
+            else:
+                ops.append(0)
+        ops.append(-1)
+        ops += [0] * ((n + B - 1) // B + 1)
+    return ops
+
+
+def main():
+    ref = ctypes.CDLL(LIB)
+    arrays = {}
+    meta = []
+    case = 0
+    for vi, variant in enumerate(VARIANTS):
+        for ki, kind in enumerate(["u32", "u64", "i32"]):
+            for si, scenario in enumerate(["sort", "concurrent", "mixed"]):
+                seed = 1000 + 97 * vi + 13 * ki + si
+                rng = np.random.default_rng(seed)
+                B = [16, 32, 64][(vi + ki + si) % 3]
+                np_variant = variant.endswith("_np")
+                # an even batch count keeps every insert of the _np variants
+                # full: a short insert there pads with init_limits keys that
+                # the bottom-up sift-down then chases past the allocation.
+                nb = 2 * int(rng.integers(6, 14))
+                n = nb * B
+                bn = 1
+                while bn * B < 2 * n:
+                    bn <<= 1
+                dt, ct, lim = TYPES[kind]
+                keys = keys_for(rng, kind, n, scenario == "concurrent")
+                ops = make_ops(rng, scenario, np_variant, B, n)
+                f = lambda name, res=ctypes.c_int: _fn(ref, variant, kind, name, res)
+                create = f("create", VP)
+                create.argtypes = [ctypes.c_int, ctypes.c_int, ct]
+                h = create(bn, B, lim)
+                out = np.zeros(n + 2 * B, dt)
+                dsizes = []
+                sz = ctypes.c_int()
+                pos = 0
+                snap_items = snap_counters = None
+                for op in ops:
+                    if op > 0:
+                        chunk = np.ascontiguousarray(keys[pos:pos + op])
+                        pos += op
+                        assert f("insert")(VP(h), VP(chunk.ctypes.data), op) == 0
+                    elif op == 0:
+                        assert f("delete")(VP(h), VP(out.ctypes.data), ctypes.byref(sz)) == 0
+                        dsizes.append(sz.value)
+                    else:
+                        snap_items = np.zeros((bn + 1) * B, dt)
+                        snap_counters = np.zeros(3, np.int32)
+                        f("state")(VP(h), VP(snap_items.ctypes.data), None, VP(snap_counters.ctypes.data))
+                        assert f("check")(VP(h)) == 1
+                items = np.zeros((bn + 1) * B, dt)
+                counters = np.zeros(3, np.int32)
+                f("state")(VP(h), VP(items.ctypes.data), None, VP(counters.ctypes.data))
+                f("destroy", None)(VP(h))
+                p = f"c{case}_"
+                arrays[p + "keys"] = keys
+                arrays[p + "ops"] = np.asarray(ops, np.int32)
+                arrays[p + "dsizes"] = np.asarray(dsizes, np.int32)
+                arrays[p + "out"] = out
+                arrays[p + "snap_items"] = snap_items
+                arrays[p + "snap_counters"] = snap_counters
+                arrays[p + "items"] = items
+                arrays[p + "counters"] = counters
+                meta.append(dict(case=case, variant=variant, topdown=variant.startswith("td"),
+                                 partial_buffer=not np_variant, key=kind, batch_size=B,
+                                 batch_num=bn, n=n, scenario=scenario, seed=seed))
+                case += 1
+    arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)
+    path = os.path.join(HERE, "bgpq_ref_cases.npz")
+    np.savez_compressed(path, **arrays)
+    print(f"wrote {case} cases to {path} ({os.path.getsize(path)} bytes)")
+
+
+def _fn(lib, variant, kind, name, res):
+    fn = getattr(lib, f"{variant}_{kind}_{name}")
+    fn.restype = res
+    return fn
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,53 @@
+"""CPU checks of the C ABI library: it loads, exports every entry point that
+include/*.h declares, and its pure host calls answer without a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_entry_points():
+    names = set()
+    for fn in os.listdir(os.path.join(REPO, "include")):
+        if fn.endswith(".h"):
+            text = open(os.path.join(REPO, "include", fn)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names |= set(re.findall(r"\b(gh_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_entry_points()
+    assert "gh_heap_create" in names and "gh_heap_sort" in names and len(names) >= 20
+
+
+@pytest.mark.parametrize("name", declared_entry_points())
+def test_library_exports(ghlib, name):
+    assert hasattr(ghlib, name), f"{name} declared in include/ but not exported"
+
+
+def test_python_binding_covers_header(ghlib):
+    import gpuheap_gb300 as gh
+    missing = set(declared_entry_points()) - set(gh._SIGS)
+    assert not missing, f"no ctypes signature for {sorted(missing)}"
+
+
+def test_host_only_calls(ghlib):
+    import gpuheap_gb300 as gh
+    assert ghlib.gh_status_string(gh.GH_ERR_TIMEOUT) == b"device wait timed out"
+    assert ghlib.gh_heap_view_bytes() == 64
+    # 3 * B keys of merge space + 64 bytes of control + 16 of alignment slack
+    assert ghlib.gh_heap_smem_bytes(0, 1024) == 3 * 1024 * 4 + 80
+    assert ghlib.gh_heap_smem_bytes(2, 1024) == 3 * 1024 * 8 + 80
+
+
+def test_rejects_bad_arguments_before_touching_a_device(ghlib):
+    h = ctypes.c_void_p()
+    assert ghlib.gh_heap_create(ctypes.byref(h), 0, 0, 1, 16, 100, None) == 1   # batch size not a power of 2
+    assert ghlib.gh_heap_create(ctypes.byref(h), 9, 0, 1, 16, 128, None) == 1   # key kind
+    assert ghlib.gh_heap_create(ctypes.byref(h), 0, 5, 1, 16, 128, None) == 1   # variant
+    assert ghlib.gh_heap_create(None, 0, 0, 1, 16, 128, None) == 1
+    assert ghlib.gh_heap_insert(None, None, 0, 0, None) == 1

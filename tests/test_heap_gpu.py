@@ -1,0 +1,259 @@
+"""GPU parity tests of the CUDA heap through the C ABI.
+
+Bar: bit-exact.  With one thread block the heap is deterministic, so its
+memory must equal the reference's own run (golden vectors) and the oracle
+model; with many concurrent blocks the deleted stream must equal std::sort
+and checkInsertHeap must hold after the insert phase (test/test.sh:5-32).
+"""
+import numpy as np
+import pytest
+
+import golden_cases
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+import gpuheap_gb300 as gh  # noqa: E402
+
+# torch views of the key types (bit patterns, no arithmetic on them)
+TORCH_VIEW = {"u32": (np.int32, torch.int32), "i32": (np.int32, torch.int32), "u64": (np.int64, torch.int64)}
+NP_KEY = {"u32": np.uint32, "i32": np.int32, "u64": np.uint64}
+
+
+def to_dev(a, key):
+    npv, _ = TORCH_VIEW[key]
+    return torch.from_numpy(np.ascontiguousarray(a).view(npv)).cuda()
+
+
+def empty_dev(n, key):
+    return torch.zeros(n, dtype=TORCH_VIEW[key][1], device="cuda")
+
+
+def to_host(t, key):
+    return t.cpu().numpy().view(NP_KEY[key])
+
+
+def batch_num_for(n, B):
+    bn = 1
+    while bn * B < 2 * n:
+        bn <<= 1
+    return bn
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda(ghlib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    yield
+
+
+@pytest.mark.parametrize("i", range(len(golden_cases.meta())))
+def test_golden_replay_single_block(i):
+    """One block replays the reference's operation list; heap memory, counters,
+    deleteRoot sizes and the HEAP_SORT stream equal the reference's run."""
+    c = golden_cases.case(i)
+    key, B = c["key"], c["batch_size"]
+    h = gh.Heap(c["batch_num"], B, key=key, variant="topdown" if c["topdown"] else "bottomup",
+                partial_buffer=c["partial_buffer"])
+    keys = to_dev(c["keys"], key)
+    out = empty_dev(c["out"].size, key)
+    pos, dsizes = 0, []
+    for op in c["ops"]:
+        if op > 0:
+            h.insertion(keys[pos:pos + op], int(op))
+            pos += op
+        elif op == 0:
+            dsizes.append(h.delete_root(out))
+        else:
+            items, status, counters = h.snapshot()
+            assert np.array_equal(counters[:3], c["snap_counters"]), "counters after the insert phase"
+            assert np.array_equal(items, c["snap_items"]), "heap memory after the insert phase"
+            assert not status.any()
+            ok, msg = h.check_insert_heap()
+            assert ok, msg
+    items, status, counters = h.snapshot()
+    assert counters[3] == 0, f"device error {counters[3:]}"
+    assert dsizes == list(c["dsizes"]), "deleteRoot sizes"
+    assert np.array_equal(to_host(out, key), c["out"]), "HEAP_SORT output"
+    assert np.array_equal(items, c["items"]), "final heap memory"
+    assert np.array_equal(counters[:3], c["counters"]), "final counters"
+    h.close()
+
+
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("pb", [True, False])
+@pytest.mark.parametrize("key,B,threads", [("u32", 256, 0), ("u32", 1024, 0), ("u32", 512, 1024),
+                                           ("u32", 512, 128), ("u64", 256, 0), ("i32", 2048, 0)])
+def test_random_ops_match_model(variant, pb, key, B, threads):
+    """Single block, random insert sizes and interleaved deletes, against the
+    oracle model: every node bit-exact at the end."""
+    rng = np.random.default_rng(B * 7 + threads + (3 if pb else 0) + (1 if variant == "topdown" else 0))
+    nb = 40
+    n = nb * B
+    bn = batch_num_for(n, B)
+    keys = pyoracle.gen(key, int(rng.integers(1 << 30)), "uniform", n)
+    h = gh.Heap(bn, B, key=key, variant=variant, partial_buffer=pb)
+    if threads:
+        h.set_block_threads(threads)
+    m = pyoracle.Model(key, variant, pb, bn, B)
+    dk = to_dev(keys, key)
+    out_d = empty_dev(n + 2 * B, key)
+    out_m = np.zeros(n + 2 * B, NP_KEY[key])
+    pos = 0
+    while True:
+        if pos < n and rng.random() < 0.6:
+            s = B if not pb else int(rng.integers(1, B + 1))
+            s = min(s, n - pos)
+            if not pb and s < B:
+                pos = n
+                continue
+            h.insertion(dk[pos:pos + s], s)
+            assert m.insert(keys[pos:pos + s]) == 0
+            pos += s
+        else:
+            a = h.delete_root(out_d)
+            b = m.delete(out_m)
+            assert a == b
+            if pos >= n and a == 0:
+                break
+    items, status, counters = h.snapshot()
+    mi, mc = m.state()
+    assert np.array_equal(items, mi)
+    assert np.array_equal(counters[:3], mc)
+    assert np.array_equal(to_host(out_d, key), out_m)
+    h.close()
+
+
+def run_heap_sort(key, variant, pb, B, n, dist="uniform", seed=1, chunk=None, grid=0):
+    keys = pyoracle.gen(key, seed, dist, n)
+    h = gh.Heap(batch_num_for(n, B), B, key=key, variant=variant, partial_buffer=pb)
+    if grid:
+        h.set_grid(grid)
+    dk = to_dev(keys, key)
+    out = empty_dev(n, key)
+    h.insert(dk, chunk=chunk if chunk is not None else (B // 3 if pb else B))
+    h.sync()
+    ok, msg = h.check_insert_heap()
+    assert ok, msg
+    assert h.item_count() == n
+    got_n = h.delete(out)
+    assert got_n == n
+    assert h.is_empty()
+    got = to_host(out, key)
+    want = pyoracle.sort(keys.copy(), threads=8)
+    h.close()
+    return got, want
+
+
+# test/test.sh:5-32: B in {128..1024} x N in {2^20, 2^21, 2^22} x the four variants
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("pb", [True, False])
+@pytest.mark.parametrize("B", [128, 256, 512, 1024])
+@pytest.mark.parametrize("logn", [20, 21, 22])
+def test_heap_sort_grid(variant, pb, B, logn):
+    n = (2**logn + B - 1) // B * B
+    got, want = run_heap_sort("u32", variant, pb, B, n, seed=logn * 131 + B)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("key", ["u64", "i32"])
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+def test_heap_sort_key_types(key, variant):
+    got, want = run_heap_sort(key, variant, True, 1024, 1 << 20, seed=3)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("dist", ["sorted", "reverse", "zipf"])
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+def test_heap_sort_distributions(dist, variant):
+    got, want = run_heap_sort("u32", variant, True, 1024, 1 << 20, dist=dist, seed=9)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("B", [256, 2048])
+def test_heap_sort_ragged_sizes(B):
+    """n not a multiple of the batch, inserts of odd sizes, partial buffer."""
+    for n, chunk in [(1, 1), (B - 1, 7), (3 * B + 5, B), (10 * B + 17, B // 3 + 1)]:
+        got, want = run_heap_sort("u32", "bottomup", True, B, n, seed=n, chunk=chunk)
+        assert np.array_equal(got, want)
+        got, want = run_heap_sort("u32", "topdown", True, B, n, seed=n + 1, chunk=chunk)
+        assert np.array_equal(got, want)
+
+
+def test_sort_entry_point():
+    n, B = (1 << 20) + 333, 1024
+    keys = pyoracle.gen("u32", 21, "uniform", n)
+    h = gh.Heap(batch_num_for(n, B), B, key="u32", variant="bottomup")
+    dk = to_dev(keys, "u32")
+    out = empty_dev(n, "u32")
+    for _ in range(2):
+        h.sort(dk, out)
+        assert np.array_equal(to_host(out, "u32"), np.sort(keys))
+    h.close()
+
+
+def test_empty_heap_and_output_limit():
+    B = 256
+    h = gh.Heap(64, B, key="u32", variant="topdown")
+    out = empty_dev(4 * B, "u32")
+    assert h.delete(out) == 0
+    assert h.delete_root(out) == 0
+    keys = pyoracle.gen("u32", 2, "uniform", 5 * B)
+    h.insert(to_dev(keys, "u32"))
+    # room for 2 batches only: stops before overflowing the output
+    assert h.delete(out, max_keys=2 * B + 10) == 2 * B
+    assert np.array_equal(to_host(out, "u32")[:2 * B], np.sort(keys)[:2 * B])
+    assert h.item_count() == 3 * B
+    h.close()
+
+
+def test_capacity_error():
+    B = 64
+    h = gh.Heap(4, B, key="u32", variant="bottomup", partial_buffer=False)
+    keys = to_dev(pyoracle.gen("u32", 4, "uniform", 6 * B), "u32")
+    h.insert(keys, n=6 * B)
+    with pytest.raises(gh.HeapError) as e:
+        h.sync()
+    assert e.value.status == gh.GH_ERR_CAPACITY
+    h.reset()
+    h.insert(keys, n=4 * B)
+    h.sync()
+    assert h.item_count() == 4 * B
+    h.close()
+
+
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+def test_bounded_wait_reports_timeout(variant):
+    """A lock word that nothing releases: the wait runs out, the kernel
+    returns, the host reads GH_ERR_TIMEOUT and the heap works after reset."""
+    B = 64
+    h = gh.Heap(16, B, key="u32", variant=variant)
+    h.set_timeout(0.05)
+    keys = to_dev(pyoracle.gen("u32", 8, "uniform", B), "u32")
+    h.inject_lock(0, 1)  # partial-buffer lock left taken
+    h.insertion(keys, B)
+    with pytest.raises(gh.HeapError) as e:
+        h.sync()
+    assert e.value.status == gh.GH_ERR_TIMEOUT
+    items, status, counters = h.snapshot()
+    assert counters[3] == gh.GH_ERR_TIMEOUT and counters[4] == 1  # partial-buffer lock site
+    h.reset()
+    h.insertion(keys, B)
+    h.sync()
+    assert h.item_count() == B
+    h.close()
+
+
+def test_invalid_arguments():
+    with pytest.raises(gh.HeapError):
+        gh.Heap(16, 100)  # not a power of two
+    with pytest.raises(gh.HeapError):
+        gh.Heap(16, 8)
+    h = gh.Heap(16, 256)
+    with pytest.raises(gh.HeapError):
+        h.set_block_threads(48)
+    with pytest.raises(gh.HeapError):
+        h.insertion(empty_dev(512, "u32"), 300)  # size > batch_size
+    h.close()

@@ -1,0 +1,192 @@
+"""CPU tests of the oracle: pinned against the reference's own heap code
+(golden vectors), the checker against planted mistakes, the generators and
+the algorithmic byte model."""
+import numpy as np
+import pytest
+
+import golden_cases
+from oracle import pyoracle
+
+N_CASES = len(golden_cases.meta())
+
+
+def replay_model(c):
+    """Runs a golden case's operation list through the oracle model."""
+    variant = "topdown" if c["topdown"] else "bottomup"
+    m = pyoracle.Model(c["key"], variant, c["partial_buffer"], c["batch_num"], c["batch_size"])
+    keys = c["keys"]
+    out = np.zeros_like(c["out"])
+    pos, dsizes, snap = 0, [], None
+    for op in c["ops"]:
+        if op > 0:
+            assert m.insert(keys[pos:pos + op]) == 0
+            pos += op
+        elif op == 0:
+            dsizes.append(m.delete(out))
+        else:
+            snap = m.state()
+    items, counters = m.state()
+    return out, np.asarray(dsizes, np.int32), snap, items, counters
+
+
+@pytest.mark.parametrize("i", range(N_CASES))
+def test_model_matches_reference_golden(i):
+    c = golden_cases.case(i)
+    out, dsizes, snap, items, counters = replay_model(c)
+    assert np.array_equal(dsizes, c["dsizes"]), "deleteRoot sizes"
+    assert np.array_equal(out, c["out"]), "HEAP_SORT output stream"
+    assert np.array_equal(snap[0], c["snap_items"]), "heap memory after the insert phase"
+    assert np.array_equal(snap[1], c["snap_counters"]), "counters after the insert phase"
+    assert np.array_equal(items, c["items"]), "final heap memory"
+    assert np.array_equal(counters, c["counters"]), "final counters"
+
+
+@pytest.mark.parametrize("i", range(N_CASES))
+def test_golden_is_a_priority_queue(i):
+    """Every deleteRoot of the reference run output the smallest keys present
+    at that moment; a pure insert-then-drain run is std::sort of the input
+    (test/heap_test.cu:163-170)."""
+    c = golden_cases.case(i)
+    keys, out = c["keys"], c["out"]
+    present = np.empty(0, keys.dtype)
+    pos = cursor = d = 0
+    for op in c["ops"]:
+        if op > 0:
+            present = np.sort(np.concatenate([present, keys[pos:pos + op]]))
+            pos += op
+        elif op == 0:
+            sz = int(c["dsizes"][d])
+            d += 1
+            assert np.array_equal(out[cursor:cursor + sz], present[:sz])
+            present = present[sz:]
+            cursor += sz
+    assert present.size == 0 and cursor == c["n"]
+    if c["scenario"] == "sort":
+        assert np.array_equal(out[:c["n"]], np.sort(keys))
+
+
+@pytest.mark.parametrize("i", [0, 7, 19, 30])
+def test_checker_accepts_golden_snapshot_and_catches_planted_mistakes(i):
+    c = golden_cases.case(i)
+    variant = "topdown" if c["topdown"] else "bottomup"
+    B = c["batch_size"]
+    items = c["snap_items"].copy()
+    bc, ps = int(c["snap_counters"][0]), int(c["snap_counters"][1])
+    status = np.zeros(c["batch_num"] + 1, np.int32)
+    assert pyoracle.check_heap(variant, items, status, B, bc, ps)
+    assert bc >= 3
+    # unsorted node
+    bad = items.copy()
+    bad[2 * B], bad[2 * B + 1] = bad[2 * B + 1], bad[2 * B]
+    if bad[2 * B] != bad[2 * B + 1]:
+        r = pyoracle.check_heap(variant, bad, status, B, bc, ps)
+        assert not r and "unsorted" in r[1]
+    # child starting below its parent's last key
+    # (node 3's parent is the root in both layouts; lowering its first key keeps it sorted)
+    bad = items.copy()
+    bad[3 * B] = bad[2 * B - 1] - 1
+    r = pyoracle.check_heap(variant, bad, status, B, bc, ps)
+    assert not r and "parent" in r[1]
+    # a lock word left taken
+    st = status.copy()
+    st[bc] = 1
+    r = pyoracle.check_heap(variant, items, st, B, bc, ps)
+    assert not r and "state" in r[1]
+
+
+def test_checker_partial_buffer_below_root():
+    B = 16
+    items = np.full(4 * B, 2**32 - 1, np.uint32)
+    items[B:2 * B] = np.arange(100, 100 + B)          # root
+    items[0:3] = [50, 60, 70]                          # partial buffer below the root
+    status = np.zeros(4, np.int32)
+    r = pyoracle.check_heap("bottomup", items, status, B, 1, 3)
+    assert not r and "partial" in r[1]
+    items[0:3] = [200, 210, 220]
+    assert pyoracle.check_heap("bottomup", items, status, B, 1, 3)
+
+
+def test_reversed_index_matches_reference_formula():
+    # heap/buitdd/heap.cuh:233-236 on the GPU: (brev(i) >> (clz(i)+1)) | (1 << (31-clz(i)))
+    def ref(i):
+        if i == 1:
+            return 1
+        clz = 32 - i.bit_length()
+        l = clz + 1
+        b = int(format(i, "032b")[::-1], 2)
+        return (b >> l) | (1 << (32 - l))
+    for i in range(1, 5000):
+        assert pyoracle.reversed_idx(i) == ref(i)
+        assert pyoracle.reversed_idx(pyoracle.reversed_idx(i)) == i
+
+
+@pytest.mark.parametrize("key", ["u32", "u64", "i32"])
+@pytest.mark.parametrize("dist", ["uniform", "sorted", "reverse", "zipf"])
+def test_generators(key, dist):
+    n = 1 << 16
+    a = pyoracle.gen(key, 11, dist, n)
+    b = pyoracle.gen(key, 11, dist, n, threads=1)
+    assert np.array_equal(a, b), "deterministic for any thread count"
+    assert not np.array_equal(a, pyoracle.gen(key, 12, dist, n))
+    init = pyoracle.INIT[key]
+    assert int(a.max()) < init
+    if dist == "sorted":
+        assert np.all(np.diff(a.astype(np.float64)) >= 0)
+    if dist == "reverse":
+        assert np.all(np.diff(a.astype(np.float64)) <= 0)
+    if key == "u64":
+        payload = (a & np.uint64(0xFFFFFFFF)).astype(np.int64)
+        assert np.array_equal(np.sort(payload), np.arange(n)), "payload is the input index"
+    if dist == "zipf":
+        hi = (a >> np.uint64(32)) if key == "u64" else a
+        vals, counts = np.unique(hi, return_counts=True)
+        assert len(vals) <= 1 << 16
+        # rank-1 share of Zipf(1.2) over 2^16 values is 1/H where H = sum r^-1.2
+        h = np.sum(np.arange(1, (1 << 16) + 1, dtype=np.float64) ** -1.2)
+        assert abs(counts.max() / n - 1.0 / h) < 0.01
+
+
+def test_uniform_covers_range():
+    a = pyoracle.gen("u32", 3, "uniform", 1 << 20)
+    assert a.min() < 2**24 and a.max() > 2**32 - 2**24
+
+
+@pytest.mark.parametrize("threads", [1, 3, 8])
+def test_parallel_sort(threads):
+    a = pyoracle.gen("u32", 5, "uniform", (1 << 20) + 7)
+    want = np.sort(a)
+    pyoracle.sort(a, threads=threads)
+    assert np.array_equal(a, want)
+
+
+@pytest.mark.parametrize("n,B,s,pb,per_key", [
+    (2**20, 1024, 4, True, 196.2), (2**28, 256, 4, True, 396.0), (2**28, 1024, 4, True, 356.0),
+    (2**28, 1024, 4, False, 340.0), (2**28, 2048, 4, True, 336.0), (2**28, 1024, 8, True, 712.0)])
+def test_sort_bytes_model(n, B, s, pb, per_key):
+    assert abs(pyoracle.sort_bytes(n, B, s, pb) / n - per_key) < 0.1
+
+
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("pb", [True, False])
+def test_model_heap_sort_random(variant, pb):
+    rng = np.random.default_rng(5)
+    B = 64
+    n = 300 * B
+    keys = rng.integers(0, 2**32 - 1, n, dtype=np.uint32)
+    m = pyoracle.Model("u32", variant, pb, 1024, B)
+    step = B // 3 if pb else B
+    for p in range(0, n, step):
+        assert m.insert(keys[p:p + step]) == 0
+    items, counters = m.state()
+    assert pyoracle.check_heap(variant, items, None, B, counters[0], counters[1])
+    out = np.zeros(n + B, np.uint32)
+    while m.delete(out):
+        pass
+    assert np.array_equal(out[:n], np.sort(keys))
+
+
+def test_model_capacity():
+    m = pyoracle.Model("u32", "topdown", False, 2, 16)
+    k = np.arange(16, dtype=np.uint32)
+    assert m.insert(k) == 0 and m.insert(k) == 0
+    assert m.insert(k) == -2
