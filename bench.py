@@ -1,0 +1,396 @@
+#!/usr/bin/env python
+"""Plain heap-sort benchmark of the GB300 batched priority queue.
+
+One step = one heap-sort through the library: reset the heap, insert all N
+keys in insertion() calls of batch_size keys over the whole grid, then
+deleteRoot/deleteUpdate until empty (test/partial_heap_test.cu:88-176 without
+its concurrent phase; artifacts/synthetic/sort.cu "insdel").  Metric: M keys/s
+insert+delete = N / (t_insert + t_delete) per step, whole job over all ranks.
+
+  value     device-resident keys: the timed region holds K back-to-back steps
+  e2e       the same through the C ABI with HOST buffers: every step copies the
+            keys in from pinned memory and the sorted keys back out
+  roofline  the dominant kernel (insert or delete drivers) against the measured
+            HBM copy bandwidth, from the closed-form algorithmic bytes
+  cpu_baseline  std::sort on the host cores (the reference tests' own CPU
+            oracle, test/heap_test.cu:121) over a bounded sample
+
+The heap path does not shard (one global root): with --gpus N every rank runs
+an independent replica and `value` sums the replicas (scaling "weak").
+
+--impl reference times the CPU implementation of the path instead (rank 0
+only): the oracle's std::sort of the same keys on all host cores.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "M keys/s insert+delete, 2^28 u32"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--log2n", type=int, default=28)
+    p.add_argument("--batch", type=int, default=2048)
+    p.add_argument("--variant", choices=["bottomup", "topdown"], default="bottomup")
+    p.add_argument("--no-partial", action="store_true")
+    p.add_argument("--key", choices=["u32", "u64"], default="u32")
+    p.add_argument("--dist", choices=["uniform", "sorted", "reverse", "zipf"], default="uniform")
+    p.add_argument("--grid", type=int, default=0, help="blocks (0: one per SM)")
+    p.add_argument("--threads", type=int, default=0, help="threads per block (0: automatic)")
+    p.add_argument("--seed", type=int, default=2026)
+    p.add_argument("--cpu-sample-log2", type=int, default=27)
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------ byte model
+def floor_log2_sum(M):
+    """sum_{k=1..M} floor(log2 k)."""
+    s, l = 0, 0
+    while (1 << l) <= M:
+        lo, hi = 1 << l, min(M, (1 << (l + 1)) - 1)
+        s += l * (hi - lo + 1)
+        l += 1
+    return s
+
+
+def algorithmic_bytes(n, B, s, pb):
+    """Closed-form BGPQ node traffic of one heap-sort, split by phase:
+    insert = s[n + sum_k 2B(L(k)+1) + pb 2BM], delete = s[n + sum_m B(1+3L(m)) + pb 2BM]."""
+    M = (n + B - 1) // B
+    SL = floor_log2_sum(M)
+    ins = s * (n + 2 * B * (SL + M) + (2 * B * M if pb else 0))
+    dele = s * (n + B * (M + 3 * SL) + (2 * B * M if pb else 0))
+    return ins, dele
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel, n, B, variant, pb):
+    """Per-launch DRAM bytes of `kernel` from profiles/traffic.json (an ncu
+    capture of a smaller case scaled by keys processed), or None."""
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            d = json.load(f)
+        e = d[f"{kernel}/{variant}/{'pb' if pb else 'np'}/B{B}"]
+        return e["dram_bytes_per_key"] * n
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU legs
+def cpu_sort_leg(log2n, seed, threads, reps):
+    """std::sort on `threads` host cores over a 2^log2n-key sample; M keys/s."""
+    import numpy as np
+    from oracle import pyoracle
+    n = 1 << log2n
+    base = pyoracle.gen("u32", seed, "uniform", n)
+    times = []
+    for _ in range(reps):
+        a = base.copy()
+        t0 = time.perf_counter()
+        pyoracle.sort(a, threads=threads)
+        times.append(time.perf_counter() - t0)
+    assert np.all(a[1:] >= a[:-1])
+    return n / statistics.median(times) / 1e6, times
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    n_sample = min(args.cpu_sample_log2, args.log2n)
+    import numpy as np
+    from oracle import pyoracle
+    n = 1 << n_sample
+    base = pyoracle.gen("u32", args.seed, args.dist, n)
+    for _ in range(args.warmup):
+        a = base.copy()
+        pyoracle.sort(a, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        a = base.copy()
+        t0 = time.perf_counter()
+        pyoracle.sort(a, threads=threads)
+        times.append(time.perf_counter() - t0)
+    assert np.all(a[1:] >= a[:-1])
+    total = sum(times)
+    value = n * len(times) / total / 1e6
+    sample = (f"std::sort (per-thread std::sort + pairwise std::merge) of 2^{n_sample} u32 {args.dist} keys "
+              f"per step on {threads} host threads; the reference has no CPU heap, its tests' CPU oracle is std::sort")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "M keys/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / len(times), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.key, "data": "synthetic",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": round(value, 3), "unit": "M keys/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "M keys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(args):
+    pb = not args.no_partial
+    name = {("bottomup", True): "buitdd", ("bottomup", False): "buitdd_np", ("topdown", True): "tditdd",
+            ("topdown", False): "tditdd_np"}[(args.variant, pb)]
+    return {"workload": f"plain heap-sort, 2^{args.log2n} {args.key} keys ({args.dist}, seeded), "
+                        f"batch_size {args.batch}, {name}, HEAP_SORT output",
+            "n_keys": 1 << args.log2n, "batch_size": args.batch, "variant": name, "key": args.key,
+            "distribution": args.dist, "global_batch": 1 << args.log2n,
+            "l2": "inputs and heap larger than L2 (129 MB); no flush needed",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+# ------------------------------------------------------------------ our arm
+def our_arm(args):
+    import numpy as np
+    import torch
+
+    import gpuheap_gb300 as gh
+    from oracle import pyoracle
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    n = 1 << args.log2n
+    B = args.batch
+    pb = not args.no_partial
+    s = 8 if args.key == "u64" else 4
+    tdt = torch.int64 if args.key == "u64" else torch.int32
+    ndt = np.int64 if args.key == "u64" else np.int32
+    bn = 1
+    while bn * B < 2 * n:
+        bn <<= 1
+
+    keys_np = pyoracle.gen(args.key, args.seed + rank, args.dist, n)
+    stream = torch.cuda.Stream()
+    keys = torch.from_numpy(keys_np.view(ndt)).cuda()
+    out = torch.empty_like(keys)
+    h = gh.Heap(bn, B, key=args.key, variant=args.variant, partial_buffer=pb)
+    if args.grid:
+        h.set_grid(args.grid)
+    if args.threads:
+        h.set_block_threads(args.threads)
+    info = h.info()
+    torch.cuda.synchronize()
+
+    def step(ev=None):
+        with torch.cuda.stream(stream):
+            if ev:
+                ev[0].record(stream)
+            h.reset_async(stream)
+            if ev:
+                ev[1].record(stream)
+            h.insert(keys, chunk=B, stream=stream)
+            if ev:
+                ev[2].record(stream)
+            h.delete(out, stream=stream, sync=False)
+            if ev:
+                ev[3].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    h.sync(stream)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = gh.launch_count()
+    barrier()
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        end.record(stream)
+        stream.synchronize()
+    barrier()
+    launches = gh.launch_count() - launches0
+    h.sync(stream)
+    total_ms = start.elapsed_time(end)
+    t_reset = [e[0].elapsed_time(e[1]) for e in evs]
+    t_ins = [e[1].elapsed_time(e[2]) for e in evs]
+    t_del = [e[2].elapsed_time(e[3]) for e in evs]
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    # correctness of the last step: sorted, and the same multiset as the input
+    got = out.cpu().numpy().view(keys_np.dtype)
+    want = pyoracle.sort(keys_np.copy(), threads=os.cpu_count() or 1)
+    if not np.array_equal(got, want):
+        raise SystemExit("bench: heap-sort output differs from std::sort")
+
+    # e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.from_numpy(keys_np.view(ndt)).pin_memory()
+        host_out = torch.empty(n, dtype=tdt).pin_memory()
+        dev_in = torch.empty_like(keys)
+        dev_out = torch.empty_like(keys)
+
+        def e2e_step():
+            with torch.cuda.stream(stream):
+                dev_in.copy_(host_in, non_blocking=True)
+                h.sort(dev_in, dev_out, stream=stream)
+                host_out.copy_(dev_out, non_blocking=True)
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            e2e_step()
+        stream.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        stream.synchronize()
+        e2e_ms = e0.elapsed_time(e1)
+        if dist is not None:
+            t = torch.tensor([e2e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        if not np.array_equal(host_out.numpy().view(keys_np.dtype), want):
+            raise SystemExit("bench: e2e output differs from std::sort")
+        e2e = {"value": round(n * ws * args.steps / (e2e_ms / 1e3) / 1e6, 3), "unit": "M keys/s",
+               "h2d_bytes_per_step": n * s, "d2h_bytes_per_step": n * s,
+               "ms_per_step": round(e2e_ms / args.steps, 3),
+               "path": "pinned host keys -> cudaMemcpyAsync -> gh_heap_sort -> pinned host output"}
+
+    value = n * ws * args.steps / (total_ms / 1e3) / 1e6
+    ins_b, del_b = algorithmic_bytes(n, B, s, pb)
+    ti, td = statistics.mean(t_ins), statistics.mean(t_del)
+    kern, kb, kt = ("k_delete", del_b, td) if td >= ti else ("k_insert", ins_b, ti)
+    peak, peak_kind = peaks()
+    achieved = kb / (kt / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 5), "traffic": ncu_traffic(kern, n, B, args.variant, pb),
+            "kernel": kern, "peak_source": f"{peak_kind} hbm_gbs",
+            "algorithmic_bytes": kb, "launch_ms": round(kt, 3),
+            "note": "achieved = closed-form BGPQ node bytes of the launch / its CUDA-event time; frac of measured"}
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "M keys/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": args.key, "data": "synthetic",
+        "config": dict(workload_config(args), block_threads=info["block_threads"], grid=info["grid"]),
+        "phases_ms": {"reset": round(statistics.mean(t_reset), 3), "insert": round(ti, 3), "delete": round(td, 3)},
+        "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
+        "whole_sort_bytes_per_key": round((ins_b + del_b) / n, 2),
+    }
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, times = cpu_sort_leg(min(args.cpu_sample_log2, args.log2n), args.seed, threads, reps=3)
+        line["cpu_baseline"] = {"value": round(v, 3), "unit": "M keys/s", "cores": threads, "kind": "port",
+                                "sample": f"std::sort of 2^{min(args.cpu_sample_log2, args.log2n)} u32 uniform keys "
+                                          f"on {threads} threads (per-thread std::sort + pairwise std::merge), "
+                                          f"median of 3"}
+    h.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return our_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -52,6 +52,7 @@ _SIGS = {
     "gh_heap_is_empty": (_I, [_VP, ctypes.POINTER(_I)]),
     "gh_heap_snapshot": (_I, [_VP, _VP, _VP, _VP]),
     "gh_heap_inject_lock": (_I, [_VP, _I, _I]),
+    "gh_launch_count": (_LL, []),
     "gh_heap_view_bytes": (ctypes.c_size_t, []),
     "gh_heap_device_view": (_I, [_VP, _VP, ctypes.c_size_t]),
     "gh_heap_smem_bytes": (ctypes.c_size_t, [_I, _I]),
@@ -82,6 +83,11 @@ def lib():
             fn.argtypes = args
         _lib = so
     return _lib
+
+
+def launch_count():
+    """Kernels launched by libgpuheap_gb300.so so far."""
+    return lib().gh_launch_count()
 
 
 class HeapError(RuntimeError):
@@ -166,6 +172,10 @@ class Heap:
         """reset(): heap/tditdd/heap.cuh:69-91."""
         _check(lib().gh_heap_reset(self._h, _stream(stream)), "reset")
         _check(lib().gh_heap_sync(self._h, _stream(stream)), "reset")
+
+    def reset_async(self, stream=None):
+        """reset() queued on `stream` without waiting."""
+        _check(lib().gh_heap_reset(self._h, _stream(stream)), "reset")
 
     # ---------------------------------------------------------------- tuning
     def set_timeout(self, seconds):

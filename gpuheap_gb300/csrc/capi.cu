@@ -16,6 +16,8 @@
 
 using gh::impl::Desc;
 
+std::atomic<long long> gh::impl::g_launches{0};
+
 struct gh_heap {
     Desc d;
     int keyKind;
@@ -94,22 +96,26 @@ gh_status fill_items(gh_heap* h, cudaStream_t s) {
         case GH_KEY_U32: {
             uint32_t v; std::memcpy(&v, &h->d.initBits, 4);
             gh::impl::k_fill<uint32_t><<<blocks, 256, 0, s>>>(static_cast<uint32_t*>(h->d.items), n, v);
+    gh::impl::count_launch();
             break;
         }
         case GH_KEY_I32: {
             int32_t v; std::memcpy(&v, &h->d.initBits, 4);
             gh::impl::k_fill<int32_t><<<blocks, 256, 0, s>>>(static_cast<int32_t*>(h->d.items), n, v);
+    gh::impl::count_launch();
             break;
         }
         default: {
             uint64_t v = h->d.initBits;
             gh::impl::k_fill<uint64_t><<<blocks, 256, 0, s>>>(static_cast<uint64_t*>(h->d.items), n, v);
+    gh::impl::count_launch();
             break;
         }
     }
     GH_CUDA(cudaGetLastError());
     GH_CUDA(cudaMemsetAsync(h->d.status, 0, sizeof(int) * (static_cast<size_t>(h->d.batchNum) + 2), s));
     gh::impl::k_init_state<<<1, 32, 0, s>>>(h->d.state, 0);
+    gh::impl::count_launch();
     GH_CUDA(cudaGetLastError());
     return GH_OK;
 }
@@ -238,6 +244,7 @@ gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long lon
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int lim = static_cast<int>(std::min<long long>(max_keys, INT_MAX));
     gh::impl::k_set_output<<<1, 32, 0, s>>>(h->d.state, 0, lim);
+    gh::impl::count_launch();
     GH_CUDA(cudaGetLastError());
     if (max_keys > 0) {
         const gh::impl::LaunchArgs a = args_of(h, s);
@@ -248,6 +255,7 @@ gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long lon
         if (st != GH_OK) return st;
     }
     gh::impl::k_set_output<<<1, 32, 0, s>>>(h->d.state, -1, INT_MAX);
+    gh::impl::count_launch();
     GH_CUDA(cudaGetLastError());
     if (n_out) {
         int dc = 0;
@@ -310,14 +318,17 @@ gh_status gh_heap_check(gh_heap* h, int* ok, char* msg, int msg_len, void* strea
         case GH_KEY_U32:
             gh::impl::k_check<uint32_t><<<blocks, 256, 0, s>>>(static_cast<const uint32_t*>(h->d.items), h->d.status,
                                                                h->d.state, h->d.variant, h->d.batchSize, h->check);
+    gh::impl::count_launch();
             break;
         case GH_KEY_I32:
             gh::impl::k_check<int32_t><<<blocks, 256, 0, s>>>(static_cast<const int32_t*>(h->d.items), h->d.status,
                                                               h->d.state, h->d.variant, h->d.batchSize, h->check);
+    gh::impl::count_launch();
             break;
         default:
             gh::impl::k_check<uint64_t><<<blocks, 256, 0, s>>>(static_cast<const uint64_t*>(h->d.items), h->d.status,
                                                                h->d.state, h->d.variant, h->d.batchSize, h->check);
+    gh::impl::count_launch();
             break;
     }
     GH_CUDA(cudaGetLastError());
@@ -388,6 +399,8 @@ gh_status gh_heap_inject_lock(gh_heap* h, int node, int state) {
     GH_CUDA(cudaMemcpy(h->d.status + node, &state, sizeof(int), cudaMemcpyHostToDevice));
     return GH_OK;
 }
+
+long long gh_launch_count(void) { return gh::impl::g_launches.load(); }
 
 size_t gh_heap_view_bytes(void) { return 64; }
 static_assert(sizeof(gh::Heap<uint64_t, 0, true>) <= 64, "device view size");

@@ -5,10 +5,16 @@
 #include <climits>
 #include <cstdint>
 
+#include <atomic>
+
 #include "gpuheap_device.cuh"
 
 namespace gh {
 namespace impl {
+
+// Kernels this library has launched (reported by gh_launch_count).
+extern std::atomic<long long> g_launches;
+inline void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 // Everything the host keeps about one heap, independent of the key type.
 struct Desc {

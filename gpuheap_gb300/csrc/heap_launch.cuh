@@ -83,6 +83,7 @@ cudaError_t launch_insert(const LaunchArgs& a, const K* keys, long long n, int c
         const long long nchunks = (n + chunk - 1) / chunk;
         const int g = static_cast<int>(nchunks < a.grid ? nchunks : a.grid);
         k_insert<H, K><<<g, a.threads, smem, a.stream>>>(h, keys, n, chunk);
+        count_launch();
         return cudaGetLastError();
     });
 }
@@ -96,6 +97,7 @@ cudaError_t launch_erase(const LaunchArgs& a, K* out) {
         cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_delete<H, K>), smem);
         if (e != cudaSuccess) return e;
         k_delete<H, K><<<a.grid, a.threads, smem, a.stream>>>(h, out);
+        count_launch();
         return cudaGetLastError();
     });
 }
@@ -109,6 +111,7 @@ cudaError_t launch_erase_one(const LaunchArgs& a, K* out) {
         cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_delete_one<H, K>), smem);
         if (e != cudaSuccess) return e;
         k_delete_one<H, K><<<1, a.threads, smem, a.stream>>>(h, out, a.opSize);
+        count_launch();
         return cudaGetLastError();
     });
 }

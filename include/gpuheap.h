@@ -122,6 +122,9 @@ gh_status gh_heap_device_view(gh_heap* h, void* view_out, size_t view_bytes);
  * (heap/tditdd/heap.cuh: 3 * batch_size keys of merge space, plus control). */
 size_t gh_heap_smem_bytes(int key_kind, int batch_size);
 
+/* Number of kernels this library has launched since it was loaded. */
+long long gh_launch_count(void);
+
 /* Properties. */
 gh_status gh_heap_info(gh_heap* h, int* key_kind, int* variant, int* partial_buffer, int* batch_num,
                        int* batch_size, int* block_threads, int* grid);
