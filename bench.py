@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--cpu-sample-log2", type=int, default=27)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--timeout", type=float, default=2.0,
+                   help="device wait limit in seconds (raise it under a profiler)")
     return p.parse_args()
 
 
@@ -259,6 +261,7 @@ def our_arm(args):
         h.set_grid(args.grid)
     if args.threads:
         h.set_block_threads(args.threads)
+    h.set_timeout(args.timeout)
     info = h.info()
     torch.cuda.synchronize()
 

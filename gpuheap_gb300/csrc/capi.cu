@@ -153,7 +153,7 @@ gh_status gh_heap_create(gh_heap** out, int key_kind, int variant, int partial_b
     if (!pow2(batch_size) || batch_size < 16 || batch_size > 4096) return GH_ERR_INVALID;
     if (batch_num < 1 || batch_num > (INT_MAX / 2 - 2)) return GH_ERR_INVALID;
     const int kb = key_bytes(key_kind);
-    if (3ull * batch_size * kb + sizeof(gh::OpCtl) + 16 > 227ull * 1024) return GH_ERR_INVALID;
+    if (gh_heap_smem_bytes(key_kind, batch_size) > 227ull * 1024) return GH_ERR_INVALID;
 
     gh_heap* h = new (std::nothrow) gh_heap();
     if (!h) return GH_ERR_INVALID;
@@ -416,7 +416,7 @@ gh_status gh_heap_device_view(gh_heap* h, void* view_out, size_t view_bytes) {
 }
 
 size_t gh_heap_smem_bytes(int key_kind, int batch_size) {
-    return 3 * static_cast<size_t>(batch_size) * key_bytes(key_kind) + sizeof(gh::OpCtl) + 16;
+    return 4 * static_cast<size_t>(batch_size) * key_bytes(key_kind) + sizeof(gh::OpCtl) + 16;
 }
 
 gh_status gh_heap_info(gh_heap* h, int* key_kind, int* variant, int* partial_buffer, int* batch_num, int* batch_size,

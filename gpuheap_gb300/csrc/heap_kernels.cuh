@@ -43,24 +43,27 @@ __global__ void __launch_bounds__(1024) k_insert(H h, const K* __restrict__ keys
     }
 }
 
-// deleteKernel: every block deletes until the heap is empty (or the output
-// limit / an error stops deleteRoot).
+// One delete: deleteRoot, then deleteUpdate when it returns true, exactly
+// as the reference's kernels call them.  Returns the number of keys written.
 template <typename H, typename K>
-__global__ void __launch_bounds__(1024) k_delete(H h, K* out) {
-    for (;;) {
-        int size = 0;
-        const bool more = h.deleteRoot(out, size);
-        if (more) h.deleteUpdate(0);
-        if (size == 0) return;
-    }
-}
-
-// One deleteRoot (+ deleteUpdate) by one block; the size goes to *sizeOut.
-template <typename H, typename K>
-__global__ void __launch_bounds__(1024) k_delete_one(H h, K* out, int* sizeOut) {
+__device__ __forceinline__ int delete_one(const H& h, K* out) {
     int size = 0;
     const bool more = h.deleteRoot(out, size);
     if (more) h.deleteUpdate(0);
+    return size;
+}
+
+// deleteKernel: every block deletes until the heap is empty (or the output
+// limit / an error stops it).
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_delete(H h, K* out) {
+    while (delete_one(h, out) != 0) {}
+}
+
+// One delete by one block; the size goes to *sizeOut.
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_delete_one(H h, K* out, int* sizeOut) {
+    const int size = delete_one(h, out);
     if (threadIdx.x == 0) *sizeOut = size;
 }
 

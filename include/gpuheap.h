@@ -119,7 +119,7 @@ size_t gh_heap_view_bytes(void);
 gh_status gh_heap_device_view(gh_heap* h, void* view_out, size_t view_bytes);
 
 /* Dynamic shared memory one block needs for the heap's operations
- * (heap/tditdd/heap.cuh: 3 * batch_size keys of merge space, plus control). */
+ * (4 * batch_size keys of node buffers plus 144 bytes of control). */
 size_t gh_heap_smem_bytes(int key_kind, int batch_size);
 
 /* Number of kernels this library has launched since it was loaded. */

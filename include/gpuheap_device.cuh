@@ -68,15 +68,16 @@ struct alignas(128) HeapState {
     int pad1[28];
 };
 
-// Per-operation control block at the end of the heap's shared-memory region.
+// Per-operation control block at the end of the heap's shared-memory region:
+// the mbarrier of the bulk copies and words that thread 0 (or the lock
+// warps) broadcast to the block.
 struct OpCtl {
     unsigned long long bar;  // mbarrier for the bulk copies
     int abort;               // block-uniform "stop" flag
     int bc, ps, dc;          // counters read under the partial-buffer lock
-    int w0, w1, w2, w3;      // broadcast words
-    int pad[6];
+    int w[26];               // broadcast words
 };
-static_assert(sizeof(OpCtl) == 64, "OpCtl layout");
+static_assert(sizeof(OpCtl) == 128, "OpCtl layout");
 
 namespace detail {
 
@@ -114,9 +115,15 @@ __device__ __forceinline__ int max_acquire(int* p, int val) {
     asm volatile("atom.acquire.gpu.global.max.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(val) : "memory");
     return old;
 }
-// Orders this thread's (and, through barriers and acquires, other threads')
-// generic-proxy global accesses before later bulk-copy (async-proxy) ones.
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async;" ::: "memory"); }
+// Orders the block's earlier generic-proxy shared-memory accesses (after a
+// barrier) before a later bulk copy (async proxy) writes the same buffers.
+// Global node data needs no proxy fence here: every node a bulk copy reads
+// was published by a fence.acq_rel.gpu + lock release, completing those
+// writes at GPU scope (in L2, where the copy engine reads) before the lock
+// word the reader acquired changed.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
@@ -160,6 +167,12 @@ __device__ __forceinline__ unsigned hi32(K k) {
     else return 0u;
 }
 
+// Bulk prefetch of `bytes` (multiple of 16, 16-byte aligned) into L2; a
+// hint with no ordering or completion to track.
+__device__ __forceinline__ void prefetch_l2(const void* src, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // Stores IPT consecutive keys from registers: 16-byte vectors when the
 // destination is 16-byte aligned and the run a multiple of 16 bytes.
 template <typename K, int IPT>
@@ -184,32 +197,53 @@ __device__ __forceinline__ void store_run(K* dst, const K (&r)[IPT]) {
     for (int q = 0; q < IPT; ++q) dst[q] = r[q];
 }
 
-// Merge-path split of two sorted runs a[0,n) and b[0,n): the n smallest keys
-// go to lo[0,n), the n largest to hi[0,n) (either may be null to discard).
-// Thread t produces outputs [t*IPT, (t+1)*IPT): a binary search on its
-// diagonal finds the split (a wins ties, as heap/heaputil.cuh:99-158 does),
-// IPT sequential merge steps fill registers, a barrier lets lo/hi alias a/b,
-// and the run is stored with vector stores.  Ends without a trailing barrier.
+// Shared-memory load through a 32-bit shared-window address.
+template <typename K>
+__device__ __forceinline__ K lds(unsigned addr) {
+    if constexpr (sizeof(K) == 4) {
+        unsigned v;
+        asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr));
+        return static_cast<K>(v);
+    } else {
+        unsigned long long v;
+        asm volatile("ld.shared.b64 %0, [%1];" : "=l"(v) : "r"(addr));
+        return static_cast<K>(v);
+    }
+}
+
+// Merge-path split of two sorted runs a[0,n) and b[0,n) held in shared
+// memory: the n smallest keys go to lo[0,n), the n largest to hi[0,n) (either
+// may be null to discard; either may be shared or global).  Thread `tid` of
+// the participating group produces outputs [tid*IPT, (tid+1)*IPT): a binary
+// search on its diagonal finds the split (a wins ties, as
+// heap/heaputil.cuh:99-158 does), IPT sequential steps fill registers, a
+// barrier lets lo/hi alias a/b, and the run is stored with vector stores.
+// Every thread of the block must call it (the barrier is block-wide); threads
+// with tid*IPT >= 2n only take part in the barrier.  No trailing barrier.
 template <typename K, int IPT>
-__device__ __forceinline__ void merge_split_t(const K* a, const K* b, K* lo, K* hi, int n) {
-    const int d = static_cast<int>(threadIdx.x) * IPT;
+__device__ __forceinline__ void merge_split_t(const K* a, const K* b, K* lo, K* hi, int n, int tid) {
+    const int d = tid * IPT;
     const bool active = d < 2 * n;
+    const unsigned sa = smem_u32(a), sb = smem_u32(b);
+    constexpr unsigned S = sizeof(K);
     K r[IPT];
     if (active) {
         int i0 = d > n ? d - n : 0, i1 = d < n ? d : n;
         while (i0 < i1) {
             const int m = (i0 + i1) >> 1;
-            if (a[m] <= b[d - 1 - m]) i0 = m + 1;
-            else i1 = m;
+            const K x = lds<K>(sa + S * m), y = lds<K>(sb + S * (d - 1 - m));
+            const bool p = x <= y;
+            i0 = p ? m + 1 : i0;
+            i1 = p ? i1 : m;
         }
         int i = i0, j = d - i0;
-        K av = a[i < n ? i : n - 1], bv = b[j < n ? j : n - 1];
+        K av = lds<K>(sa + S * (i < n ? i : n - 1)), bv = lds<K>(sb + S * (j < n ? j : n - 1));
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
             const bool ta = (j >= n) || (i < n && av <= bv);
             r[k] = ta ? av : bv;
-            if (ta) { ++i; av = a[i < n ? i : n - 1]; }
-            else { ++j; bv = b[j < n ? j : n - 1]; }
+            if (ta) { ++i; av = lds<K>(sa + S * (i < n ? i : n - 1)); }
+            else { ++j; bv = lds<K>(sb + S * (j < n ? j : n - 1)); }
         }
     }
     __syncthreads();
@@ -219,20 +253,15 @@ __device__ __forceinline__ void merge_split_t(const K* a, const K* b, K* lo, K* 
     }
 }
 
-template <typename K, int FIXED_IPT = 0>
-__device__ __forceinline__ void merge_split(const K* a, const K* b, K* lo, K* hi, int n) {
-    if constexpr (FIXED_IPT > 0) {
-        merge_split_t<K, FIXED_IPT>(a, b, lo, hi, n);
-        return;
-    }
-    int ipt = (2 * n) / static_cast<int>(blockDim.x);
-    if (ipt < 1) ipt = 1;
+// Run-time IPT (= 2n*groups/blockDim) dispatch for callers without a fixed one.
+template <typename K>
+__device__ __forceinline__ void merge_split_rt(const K* a, const K* b, K* lo, K* hi, int n, int tid, int ipt) {
     switch (ipt) {
-        case 1: merge_split_t<K, 1>(a, b, lo, hi, n); break;
-        case 2: merge_split_t<K, 2>(a, b, lo, hi, n); break;
-        case 4: merge_split_t<K, 4>(a, b, lo, hi, n); break;
-        case 8: merge_split_t<K, 8>(a, b, lo, hi, n); break;
-        default: merge_split_t<K, 16>(a, b, lo, hi, n); break;
+        case 1: merge_split_t<K, 1>(a, b, lo, hi, n, tid); break;
+        case 2: merge_split_t<K, 2>(a, b, lo, hi, n, tid); break;
+        case 4: merge_split_t<K, 4>(a, b, lo, hi, n, tid); break;
+        case 8: merge_split_t<K, 8>(a, b, lo, hi, n, tid); break;
+        default: merge_split_t<K, 16>(a, b, lo, hi, n, tid); break;
     }
 }
 
@@ -283,9 +312,15 @@ struct Heap {
     int sortOutput;        // 1: HEAP_SORT output at items + deleteCount
     long long timeoutNs;   // bound on every wait
 
+    // Four node buffers in shared memory: the carried batch (or insert
+    // batch), the partial buffer (or loaded node) and the two children.
+    static constexpr int kBufs = 4;
     static __host__ __device__ size_t smemBytes(int bs) {
-        return 3 * static_cast<size_t>(bs) * sizeof(K) + sizeof(OpCtl) + 16;
+        return kBufs * static_cast<size_t>(bs) * sizeof(K) + sizeof(OpCtl) + 16;
     }
+
+    // Kid ownership after an acquire attempt.
+    static constexpr int kAbsent = 0, kHeld = 1, kPending = 2;
 
     // ------------------------------------------------------------------ plumbing
     __device__ __forceinline__ K* region(int smemOffset) const {
@@ -293,9 +328,24 @@ struct Heap {
         size_t off = (static_cast<size_t>(smemOffset) * 4 + 15) & ~static_cast<size_t>(15);
         return reinterpret_cast<K*>(gh_dyn_smem + off);
     }
-    __device__ __forceinline__ OpCtl* ctl(K* base) const { return reinterpret_cast<OpCtl*>(base + 3 * batchSize); }
+    __device__ __forceinline__ OpCtl* ctl(K* base) const { return reinterpret_cast<OpCtl*>(base + kBufs * batchSize); }
     __device__ __forceinline__ K* node(int i) const { return heapItems + static_cast<size_t>(i) * batchSize; }
     __device__ __forceinline__ unsigned nodeBytes() const { return static_cast<unsigned>(batchSize * sizeof(K)); }
+    __device__ __forceinline__ static constexpr int lockedState() { return VARIANT == kTopDown ? TD::INUSE : BU::INUSE; }
+    // Thread that runs the q-th of up to three concurrent lock waits: one per
+    // warp when the block has three warps, else thread 0 for all.
+    __device__ __forceinline__ int lockThread(int q) const { return blockDim.x >= 96 ? 32 * q : 0; }
+
+    // Merge of two sorted batches; G = 2 splits the block into two groups
+    // that merge two independent pairs at once.
+    template <int G>
+    __device__ __forceinline__ void mergeG(const K* a, const K* b, K* lo, K* hi, int tid) const {
+        if constexpr (IPT > 0) detail::merge_split_t<K, IPT * G>(a, b, lo, hi, batchSize, tid);
+        else detail::merge_split_rt<K>(a, b, lo, hi, batchSize, tid, (2 * batchSize * G) / static_cast<int>(blockDim.x));
+    }
+    __device__ __forceinline__ void merge(const K* a, const K* b, K* lo, K* hi) const {
+        mergeG<1>(a, b, lo, hi, static_cast<int>(threadIdx.x));
+    }
 
     // Records the first error (sticky).
     __device__ __forceinline__ void raise(int code, int site, int nodeIdx, int seen) const {
@@ -309,7 +359,8 @@ struct Heap {
 
     // Periodic check inside a wait: false once the time limit has passed
     // (the error is raised) or another block has already raised one.
-    __device__ __forceinline__ bool keep_waiting(unsigned long long& t0, unsigned it, int site, int nodeIdx, int seen) const {
+    __device__ __forceinline__ bool keep_waiting(unsigned long long& t0, unsigned it, int site, int nodeIdx,
+                                                 int seen) const {
         if ((it & 15u) != 15u) return true;
         const unsigned long long now = detail::globaltimer();
         if (t0 == 0) t0 = now;
@@ -321,62 +372,119 @@ struct Heap {
         return true;
     }
 
-    // Spin until status[i] == from, then swap in `to` with acquire semantics.
+    // Swap status[i] from `from` to `to` (acquire); CAS first, then poll
+    // until the word looks free and retry.
     __device__ __forceinline__ bool lock(int i, int from, int to, int site) const {
         int* w = status + i;
         unsigned long long t0 = 0;
-        for (unsigned it = 0;; ++it) {
-            const int v = detail::ld_relaxed(w);
-            if (v == from && detail::cas_acquire(w, from, to) == from) return true;
-            if (!keep_waiting(t0, it, site, i, v)) return false;
+        unsigned it = 0;
+        for (;;) {
+            int v = detail::cas_acquire(w, from, to);
+            if (v == from) return true;
+            do {
+                if (!keep_waiting(t0, it++, site, i, v)) return false;
+                v = detail::ld_relaxed(w);
+            } while (v != from);
         }
     }
-    // Owner-side transition out of an exclusive state.
+    // Owner-side transition out of an exclusive state (release).
     __device__ __forceinline__ void unlock(int i, int to) const { detail::st_release(status + i, to); }
+    // After fence(): plain transitions, ordered by that fence.
+    __device__ __forceinline__ static void fence() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+    __device__ __forceinline__ void setState(int i, int to) const { detail::st_relaxed(status + i, to); }
 
-    // Block-wide setup: fresh mbarrier, abort if the heap already failed.
+    // One attempt at a child: held (prev = state to restore), pending (held by
+    // someone else) or absent (outside the allocation, or an insert target).
+    __device__ __forceinline__ int tryChild(int x, int& prev) const {
+        prev = 0;
+        if (x > batchNum) return kAbsent;
+        if constexpr (VARIANT == kTopDown) {
+            const int v = detail::cas_acquire(status + x, TD::AVAIL, TD::INUSE);
+            if (v == TD::AVAIL) return kHeld;
+            return v == TD::INUSE ? kPending : kAbsent;
+        } else {
+            // heap/buitdd/heap.cuh:409-418: atomicMax takes AVAIL, INSHOLD or
+            // DELMOD; a node a bubbling insert holds (INSHOLD) goes back as DELMOD.
+            const int v = detail::max_acquire(status + x, BU::INUSE);
+            if (v == BU::INUSE) return kPending;
+            prev = v == BU::INSHOLD ? BU::DELMOD : v;
+            return kHeld;
+        }
+    }
+    // Blocking version: held or absent, or -1 on timeout.
+    __device__ __forceinline__ int takeChild(int x, int& prev) const {
+        unsigned long long t0 = 0;
+        for (unsigned it = 0;; ++it) {
+            const int r = tryChild(x, prev);
+            if (r != kPending) return r;
+            if (!keep_waiting(t0, it, kSiteLockChild, x, lockedState())) return -1;
+            if constexpr (VARIANT == kTopDown) {
+                // poll before the next CAS
+                while (detail::ld_relaxed(status + x) == TD::INUSE) {
+                    if (!keep_waiting(t0, ++it, kSiteLockChild, x, TD::INUSE)) return -1;
+                }
+            }
+        }
+    }
+
+    // Block-wide bulk-copy bookkeeping on one mbarrier; only thread 0 issues
+    // and waits, the others meet it at a barrier.
     struct Op {
         const Heap* h;
         OpCtl* c;
         unsigned phase;
-        __device__ __forceinline__ Op(const Heap* hp, OpCtl* cp) : h(hp), c(cp), phase(0) {
+        bool inflight;
+        __device__ __forceinline__ Op(const Heap* hp, OpCtl* cp) : h(hp), c(cp), phase(0), inflight(false) {
             __syncthreads();
             if (threadIdx.x == 0) {
-                c->abort = detail::ld_relaxed(&h->state->err) != 0;
+                c->abort = 0;
                 detail::mbar_init(&c->bar, 1);
             }
             __syncthreads();
         }
         __device__ __forceinline__ ~Op() {
+            if (threadIdx.x == 0 && inflight) drain();
             __syncthreads();
             if (threadIdx.x == 0) detail::mbar_inval(&c->bar);
         }
-        // Thread 0 only: start one bulk transaction of `bytes`.
-        __device__ __forceinline__ void expect(unsigned bytes) {
-            detail::fence_proxy_async();
+        // Thread 0: start one transaction of `bytes` (copies follow).
+        __device__ __forceinline__ void issue(unsigned bytes) {
+            detail::fence_proxy_async_smem();
             detail::mbar_arrive_expect_tx(&c->bar, bytes);
+            inflight = true;
         }
-        // Block-wide: thread 0 waits for the transaction (bounded), the rest
-        // wait at the barrier.  Returns false (block-uniform) on failure.
-        __device__ __forceinline__ bool wait() {
-            if (threadIdx.x == 0) {
-                unsigned long long t0 = 0;
-                bool ok = true;
-                for (unsigned it = 0; !detail::mbar_try_wait(&c->bar, phase); ++it) {
-                    if (!h->keep_waiting(t0, it, kSiteBulkCopy, -1, 0)) { ok = false; break; }
-                }
-                if (!ok) {
-                    // The copies read valid global memory and must land before the
-                    // shared memory is reused: give them a second bounded wait.
-                    for (unsigned it = 0; it < (1u << 22) && !detail::mbar_try_wait(&c->bar, phase); ++it) {}
-                    c->abort = 1;
+        // Thread 0: wait for the transaction in flight (bounded).
+        __device__ __forceinline__ bool wait0() {
+            if (!inflight) return true;
+            unsigned long long t0 = 0;
+            for (unsigned it = 0; !detail::mbar_try_wait(&c->bar, phase); ++it) {
+                if (!h->keep_waiting(t0, it, kSiteBulkCopy, -1, 0)) {
+                    drain();
+                    return false;
                 }
             }
             phase ^= 1u;
+            inflight = false;
+            return true;
+        }
+        // The copies read valid global memory and land in this block's shared
+        // memory: give them a second bounded wait before it is reused.
+        __device__ __forceinline__ void drain() {
+            for (unsigned it = 0; it < (1u << 22) && !detail::mbar_try_wait(&c->bar, phase); ++it) {}
+            phase ^= 1u;
+            inflight = false;
+        }
+        // Block-wide wait; false (block-uniform) on failure.
+        __device__ __forceinline__ bool wait() {
+            if (threadIdx.x == 0 && !wait0()) c->abort = 1;
             __syncthreads();
             return !c->abort;
         }
     };
+
+    __device__ __forceinline__ void load(K* dst, int i, unsigned long long* bar) const {
+        detail::bulk_g2s(dst, node(i), nodeBytes(), bar);
+    }
 
     // Block-wide copies between shared and global nodes (16-byte aligned).
     __device__ __forceinline__ void store_node(int i, const K* s) const {
@@ -385,7 +493,7 @@ struct Heap {
         const uint4* v = reinterpret_cast<const uint4*>(s);
         for (int q = threadIdx.x; q < nv; q += blockDim.x) g[q] = v[q];
     }
-    __device__ __forceinline__ void fill_node(int i, int count) const {  // first `count` keys (multiple of 16 B) or scalar tail
+    __device__ __forceinline__ void fill_node(int i, int count) const {
         K* g = node(i);
         const int per = 16 / static_cast<int>(sizeof(K));
         const int nv = count / per;
@@ -407,8 +515,8 @@ struct Heap {
         }
     }
 
-    // Node layout helpers.  Bottom-up heaps store level-order nodes with the
-    // bits below the leading one reversed (heap/buitdd/heap.cuh:233-236).
+    // Node layout.  Bottom-up heaps store level-order nodes with the bits
+    // below the leading one reversed (heap/buitdd/heap.cuh:233-236).
     __device__ __forceinline__ static int rev(int i) {
         if (i <= 1) return i;
         const int l = __clz(i) + 1;
@@ -421,6 +529,7 @@ struct Heap {
     __device__ __forceinline__ static int nextOnPath(int cur, int target) {
         return target >> (__clz(cur) - __clz(target) - 1);
     }
+    __device__ __forceinline__ int rightOrNone(int l) const { return l <= batchNum ? rightOf(l) : batchNum + 1; }
 
     // ------------------------------------------------------------------ insertion
     // heap/tditdd/heap.cuh:536-753 (top-down) and heap/buitdd/heap.cuh:484-690
@@ -431,7 +540,6 @@ struct Heap {
         K* s2 = s1 + batchSize;
         Op op(this, ctl(s0));
         OpCtl* c = op.c;
-        if (c->abort) return;
         const int B = batchSize;
         const int tid = threadIdx.x;
 
@@ -440,13 +548,15 @@ struct Heap {
         __syncthreads();
         detail::bitonic_sort(s0, B);
 
-        // lock the partial buffer; the counters are only changed under it
+        // lock the partial buffer (the counters are only changed under it) and
+        // start loading it
         if (tid == 0) {
             const bool ok = lock(0, 0, lockedState(), kSiteLockPartial);
             c->abort = !ok;
             if (ok) {
                 c->bc = detail::ld_relaxed(&state->batchCount);
                 c->ps = detail::ld_relaxed(&state->partialBufferSize);
+                if (PB) { op.issue(nodeBytes()); load(s1, 0, &c->bar); }
             }
         }
         __syncthreads();
@@ -454,6 +564,7 @@ struct Heap {
         const int bc = c->bc, ps = c->ps;
 
         if constexpr (PB) {
+            if (!op.wait()) return;
             if (bc == 0 && size < B) {
                 if (ps == 0) {  // case 1.1 (:575-584)
                     store_node(0, s0);
@@ -464,10 +575,8 @@ struct Heap {
                     }
                     return;
                 }
-                if (tid == 0) { op.expect(nodeBytes()); detail::bulk_g2s(s1, node(0), nodeBytes(), &c->bar); }
-                if (!op.wait()) return;
                 if (size + ps < B) {  // case 1.2 (:586-598)
-                    detail::merge_split<K, IPT>(s0, s1, node(0), static_cast<K*>(nullptr), B);
+                    merge(s0, s1, node(0), static_cast<K*>(nullptr));
                     __syncthreads();
                     if (tid == 0) {
                         detail::st_relaxed(&state->partialBufferSize, ps + size);
@@ -485,52 +594,53 @@ struct Heap {
                 }
                 __syncthreads();
                 if (c->abort) return;
-                detail::merge_split<K, IPT>(s0, s1, node(1), node(0), B);
+                merge(s0, s1, node(1), node(0));
                 __syncthreads();
                 if (tid == 0) {
                     detail::st_relaxed(&state->partialBufferSize, ps + size - B);
-                    unlock(0, 0);
-                    unlock(1, 0);
+                    fence();
+                    setState(0, 0);
+                    setState(1, 0);
                 }
                 return;
             }
-            if (tid == 0) { op.expect(nodeBytes()); detail::bulk_g2s(s1, node(0), nodeBytes(), &c->bar); }
-            if (!op.wait()) return;
             if (size + ps < B) {  // case 2.1 (:625-648): no new full batch, merge through the root
-                detail::merge_split<K, IPT>(s0, s1, s0, static_cast<K*>(nullptr), B);
+                merge(s0, s1, s0, static_cast<K*>(nullptr));
                 __syncthreads();
                 if (tid == 0) {
                     const bool ok = lock(1, 0, lockedState(), kSiteLockRoot);
                     c->abort = !ok;
-                    if (ok) { op.expect(nodeBytes()); detail::bulk_g2s(s1, node(1), nodeBytes(), &c->bar); }
+                    if (ok) { op.issue(nodeBytes()); load(s1, 1, &c->bar); }
                 }
                 __syncthreads();
                 if (c->abort) return;
                 if (!op.wait()) return;
-                detail::merge_split<K, IPT>(s0, s1, node(1), node(0), B);
+                merge(s0, s1, node(1), node(0));
                 __syncthreads();
                 if (tid == 0) {
                     detail::st_relaxed(&state->partialBufferSize, ps + size);
-                    unlock(0, 0);
-                    unlock(1, 0);
+                    fence();
+                    setState(0, 0);
+                    setState(1, 0);
                 }
                 return;
             }
             // case 2.2 (:650-662): the smaller B keys go on, the rest stay in node 0
-            detail::merge_split<K, IPT>(s0, s1, s0, node(0), B);
+            merge(s0, s1, s0, node(0));
             __syncthreads();
             if (tid == 0) detail::st_relaxed(&state->partialBufferSize, ps + size - B);
         }
 
-        if constexpr (VARIANT == kTopDown) insert_topdown(op, s0, s1, bc);
+        if constexpr (VARIANT == kTopDown) insert_topdown(op, s0, s1, s2, bc);
         else insert_bottomup(op, s0, s1, s2, bc);
     }
 
-    __device__ __forceinline__ static constexpr int lockedState() { return VARIANT == kTopDown ? TD::INUSE : BU::INUSE; }
-
     // Top-down path (heap/tditdd/heap.cuh:666-752).  Entered holding node 0;
-    // the carried batch is in s0.
-    __device__ __forceinline__ void insert_topdown(Op& op, K* s0, K* s1, int bc) const {
+    // the carried batch is in s0.  Each node on the root -> target path is
+    // held while its merge runs; the next node is locked and its load started
+    // before this one is released (locking it before the merge measured
+    // slower: it lengthens the hold).
+    __device__ __forceinline__ void insert_topdown(Op& op, K* s0, K* s1, K* s2, int bc) const {
         OpCtl* c = op.c;
         const int tid = threadIdx.x;
         if (tid == 0) {
@@ -539,63 +649,81 @@ struct Heap {
             if (!ok) raise(kErrCapacity, kSiteCapacity, target, 0);
             if (ok) detail::st_relaxed(&state->batchCount, target);
             ok = ok && lock(target, TD::AVAIL, TD::TARGET, kSiteLockTarget);
-            if (ok && target != 1) ok = lock(1, TD::AVAIL, TD::INUSE, kSiteLockRoot);
+            if (ok && target != 1) {
+                ok = lock(1, TD::AVAIL, TD::INUSE, kSiteLockRoot);
+                if (ok) { op.issue(nodeBytes()); load(s1, 1, &c->bar); }
+            }
+            // the root is ours: release the partial buffer (the reference does
+            // this at the top of the first path step, :692-694)
+            if (ok) unlock(0, TD::AVAIL);
             c->abort = !ok;
-            c->w0 = target;
+            c->w[0] = target;
         }
         __syncthreads();
         if (c->abort) return;
-        const int target = c->w0;
+        const int target = c->w[0];
         int cur = 1;
+        K* cn = s1;  // current node's keys
+        K* nx = s2;  // next node's keys
         while (cur != target) {
+            const int next = nextOnPath(cur, target);
             if (tid == 0) {
-                c->w1 = detail::ld_relaxed(status + target) == TD::MARKED;
-                if (!c->w1) {
-                    unlock(cur >> 1, TD::AVAIL);  // hand-over-hand: release the parent
-                    op.expect(nodeBytes());
-                    detail::bulk_g2s(s1, node(cur), nodeBytes(), &c->bar);
-                }
+                // (:683-689) a deleter that took the target waits for this batch at the root
+                c->w[1] = detail::ld_relaxed(status + target) == TD::MARKED;
+                if (!c->w[1] && !op.wait0()) c->abort = 1;
             }
             __syncthreads();
-            if (c->w1) break;  // a deleter has taken the target (:683-689)
-            if (!op.wait()) return;
-            detail::merge_split<K, IPT>(s0, s1, node(cur), s0, batchSize);
-            cur = nextOnPath(cur, target);
+            if (c->abort) return;
+            if (c->w[1]) break;
+            merge(s0, cn, node(cur), s0);
             __syncthreads();
-            if (tid == 0 && cur != target) c->abort = !lock(cur, TD::AVAIL, TD::INUSE, kSiteLockPath);
+            if (tid == 0) {
+                bool ok = true;
+                if (next != target) {
+                    ok = lock(next, TD::AVAIL, TD::INUSE, kSiteLockPath);
+                    if (ok) { op.issue(nodeBytes()); load(nx, next, &c->bar); }
+                }
+                fence();
+                setState(cur, TD::AVAIL);
+                c->abort = !ok;
+            }
             __syncthreads();
             if (c->abort) return;
+            cur = next;
+            K* t = cn; cn = nx; nx = t;
         }
         if (tid == 0) {
             const int old = detail::cas_acq_rel(status + target, TD::TARGET, TD::INUSE);
-            c->w2 = old == TD::MARKED;
+            c->w[3] = old == TD::MARKED;
         }
         __syncthreads();
-        if (c->w2) {
-            // The deleter that marked the target holds the root and waits for
-            // this batch there (:732-744).
+        if (c->w[3] || (cur != target)) {
+            // (:732-744) the deleter that marked the target holds the root and
+            // waits for this batch there
             store_node(1, s0);
             __syncthreads();
             if (tid == 0) {
-                unlock(cur >> 1, TD::AVAIL);
-                if (target != cur) unlock(cur, TD::AVAIL);
-                unlock(target, TD::TARGET);  // MARKED -> TARGET, release
+                fence();
+                if (cur != target) setState(cur, TD::AVAIL);
+                setState(target, TD::TARGET);  // MARKED -> TARGET
             }
             return;
         }
         store_node(target, s0);
         __syncthreads();
-        if (tid == 0) {
-            unlock(cur >> 1, TD::AVAIL);
-            unlock(cur, TD::AVAIL);
-        }
+        if (tid == 0) unlock(target, TD::AVAIL);
     }
 
     // Bottom-up path (heap/buitdd/heap.cuh:616-689).  Entered holding node 0;
-    // the carried batch is in s0.
+    // the carried batch is in s0.  The reference parks its node as INSHOLD
+    // before waiting for the parent; here one attempt at the parent comes
+    // first and the park only happens when that attempt fails.  A level whose
+    // parent already ends at or below the batch changes nothing, and neither
+    // would any level above it, so the walk stops there.
     __device__ __forceinline__ void insert_bottomup(Op& op, K* s0, K* s1, K* s2, int bc) const {
         OpCtl* c = op.c;
         const int tid = threadIdx.x;
+        const int B = batchSize;
         if (tid == 0) {
             const int target = bc + 1;
             bool ok = target <= batchNum;
@@ -604,51 +732,66 @@ struct Heap {
             ok = ok && lock(target, BU::AVAIL, BU::INUSE, kSiteLockTarget);
             if (ok) unlock(0, BU::AVAIL);
             c->abort = !ok;
-            c->w0 = target;
+            c->w[0] = target;
         }
         __syncthreads();
         if (c->abort) return;
-        int cur = c->w0;
+        int cur = c->w[0];
         store_node(cur, s0);
         __syncthreads();
-        if (tid == 0) unlock(cur, BU::INSHOLD);
+        K* carried = s0;
+        K* spare = s2;
         while (cur != 1) {
             const int p = parentOf(cur);
             if (tid == 0) {
-                bool ok = lock(p, BU::AVAIL, BU::INUSE, kSiteLockPath);
-                if (ok) {
-                    // take our own node back from INSHOLD (or DELMOD if a
-                    // deleter rewrote it meanwhile)
-                    unsigned long long t0 = 0;
-                    int prev;
-                    for (unsigned it = 0; (prev = detail::max_acquire(status + cur, BU::INUSE)) == BU::INUSE; ++it) {
-                        if (!keep_waiting(t0, it, kSiteLockPath, cur, prev)) { ok = false; break; }
+                bool ok = true;
+                int reload = 0;
+                if (detail::cas_acquire(status + p, BU::AVAIL, BU::INUSE) != BU::AVAIL) {
+                    // park our node so a deleter can pass through it, then wait
+                    fence();
+                    setState(cur, BU::INSHOLD);
+                    ok = lock(p, BU::AVAIL, BU::INUSE, kSiteLockPath);
+                    if (ok) {
+                        unsigned long long t0 = 0;
+                        int prev;
+                        for (unsigned it = 0; (prev = detail::max_acquire(status + cur, BU::INUSE)) == BU::INUSE; ++it) {
+                            if (!keep_waiting(t0, it, kSiteLockPath, cur, prev)) { ok = false; break; }
+                        }
+                        reload = ok && prev != BU::INSHOLD;  // a deleter rewrote it meanwhile
                     }
                 }
-                c->abort = !ok;
                 if (ok) {
-                    op.expect(2 * nodeBytes());
-                    detail::bulk_g2s(s1, node(p), nodeBytes(), &c->bar);
-                    detail::bulk_g2s(s2, node(cur), nodeBytes(), &c->bar);
+                    op.issue((reload ? 2u : 1u) * nodeBytes());
+                    load(s1, p, &c->bar);
+                    if (reload) load(carried, cur, &c->bar);
                 }
+                c->abort = !ok;
             }
             __syncthreads();
             if (c->abort) return;
             if (!op.wait()) return;
-            if (s1[0] >= s2[batchSize - 1]) {  // whole batch below the parent: swap (:647-661)
-                store_node(p, s2);
+            int done = 0;
+            if (s1[0] >= carried[B - 1]) {  // whole batch below the parent: swap (:647-661)
+                store_node(p, carried);
                 store_node(cur, s1);
+            } else if (s1[B - 1] <= carried[0]) {
+                done = 1;  // already ordered: nothing changes here or above
             } else {
-                detail::merge_split<K, IPT>(s2, s1, node(p), node(cur), batchSize);
+                merge(carried, s1, spare, node(cur));
+                __syncthreads();
+                store_node(p, spare);
+                K* t = carried; carried = spare; spare = t;
             }
             __syncthreads();
             if (tid == 0) {
-                unlock(p, BU::INSHOLD);
-                unlock(cur, BU::AVAIL);
+                fence();
+                setState(cur, BU::AVAIL);
+                if (done) setState(p, BU::AVAIL);
             }
+            if (done) return;
             cur = p;
         }
-        if (tid == 0) unlock(1, BU::AVAIL);  // INSHOLD -> INUSE -> AVAIL (:685-688)
+        if (tid == 0) unlock(1, BU::AVAIL);  // (:685-688)
     }
 
     // ------------------------------------------------------------------ deleteRoot
@@ -666,9 +809,8 @@ struct Heap {
         const int L = lockedState();
         __syncthreads();
         if (tid == 0) {
-            c->abort = detail::ld_relaxed(&state->err) != 0;
-            c->w0 = 0;  // 0: nothing, 1: partial buffer only, 2: root
-            const bool ok = !c->abort && lock(0, 0, L, kSiteLockPartial);
+            c->w[0] = 0;  // 0: nothing, 1: partial buffer only, 2: root
+            const bool ok = detail::ld_relaxed(&state->err) == 0 && lock(0, 0, L, kSiteLockPartial);
             c->abort = !ok;
             if (ok) {
                 const int bc = detail::ld_relaxed(&state->batchCount);
@@ -680,34 +822,29 @@ struct Heap {
                 if (want == 0 || (sortOutput && dc + want > lim)) {
                     unlock(0, 0);
                 } else if (bc == 0) {
-                    c->w0 = 1;
+                    c->w[0] = 1;
                 } else {
+                    // deleteUpdate will take node bc (a leaf, usually not in
+                    // L2): start pulling it in while this block waits for the root
+                    if (bc > 1) detail::prefetch_l2(node(bc), nodeBytes());
                     const bool ok1 = lock(1, 0, L, kSiteLockRoot);
                     c->abort = !ok1;
                     if (ok1) {
-                        c->w0 = 2;
+                        c->w[0] = 2;
                         if (sortOutput) detail::st_relaxed(&state->deleteCount, dc + batchSize);
                     }
                 }
             }
         }
         __syncthreads();
-        const int mode = c->w0;
+        const int mode = c->w[0];
         const bool stop = c->abort || mode == 0;
         const int dc = c->dc, ps = c->ps;
         __syncthreads();  // every thread has read dr before the next call rewrites it
         if (stop) return false;
         K* out = items + (sortOutput ? dc : 0);
-        if (mode == 1) {  // only the partial buffer holds keys (:297-315)
-            copy_out(out, 0, ps);
-            __syncthreads();
-            fill_node(0, ps);
-            __syncthreads();
-            if (tid == 0) {
-                if (sortOutput) detail::st_relaxed(&state->deleteCount, dc + ps);
-                detail::st_relaxed(&state->partialBufferSize, 0);
-                unlock(0, 0);
-            }
+        if (mode == 1) {
+            partial_out(out, ps, dc);
             size = ps;
             return false;
         }
@@ -717,233 +854,182 @@ struct Heap {
         return true;
     }
 
+    // Only the partial buffer holds keys (:297-315): output and reset it,
+    // release node 0.
+    __device__ __forceinline__ void partial_out(K* out, int ps, int dc) const {
+        copy_out(out, 0, ps);
+        __syncthreads();
+        fill_node(0, ps);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (sortOutput) detail::st_relaxed(&state->deleteCount, dc + ps);
+            detail::st_relaxed(&state->partialBufferSize, 0);
+            unlock(0, 0);
+        }
+    }
+
     // ------------------------------------------------------------------ deleteUpdate
     // Refills the root: heap/tditdd/heap.cuh:345-534, heap/buitdd/heap.cuh:348-482.
     __device__ __forceinline__ void deleteUpdate(int smemOffset) const {
-        K* s0 = region(smemOffset);
-        K* s1 = s0 + batchSize;
-        K* s2 = s1 + batchSize;
-        Op op(this, ctl(s0));
+        K* base = region(smemOffset);
+        Op op(this, ctl(base));
         OpCtl* c = op.c;
-        if (c->abort) return;
-        const int tid = threadIdx.x;
-        const int B = batchSize;
-        const int L = lockedState();
-
-        // take the last node (:355-369)
-        if (tid == 0) {
+        if (threadIdx.x == 0) {
             const int last = detail::ld_relaxed(&state->batchCount);
             detail::st_relaxed(&state->batchCount, last - 1);
-            c->w0 = last;
-            c->w1 = 0;  // 0: last node taken, 1: in-flight insert handed its batch to the root
-            if (last == 1) {
-                unlock(1, 0);
-                unlock(0, 0);
-            } else if (VARIANT == kTopDown) {
-                // (:371-402) either lock it, or mark an in-flight insert target
-                unsigned long long t0 = 0;
-                bool ok = true;
-                for (unsigned it = 0;; ++it) {
-                    if (detail::cas_acquire(status + last, TD::AVAIL, TD::INUSE) == TD::AVAIL) break;
-                    if (detail::cas_acquire(status + last, TD::TARGET, TD::MARKED) == TD::TARGET) { c->w1 = 1; break; }
-                    if (!keep_waiting(t0, it, kSiteLockLast, last, detail::ld_relaxed(status + last))) { ok = false; break; }
-                }
-                if (ok && c->w1) {
-                    t0 = 0;
-                    for (unsigned it = 0; detail::cas_acquire(status + last, TD::TARGET, TD::AVAIL) != TD::TARGET; ++it) {
-                        if (!keep_waiting(t0, it, kSiteHandOff, last, detail::ld_relaxed(status + last))) { ok = false; break; }
-                    }
-                }
-                c->abort = !ok;
+            c->w[0] = last;
+        }
+        __syncthreads();
+        const int last = c->w[0];
+        if (last == 1) {  // (:357-369) the root was the only full node
+            if (threadIdx.x == 0) { unlock(1, 0); unlock(0, 0); }
+            return;
+        }
+        refill_and_sift(op, base, last);
+    }
+
+    // The children of the node at one level, after they are locked and loaded.
+    struct Level {
+        int have, l, r, lPrev, rPrev, larger, smaller, lp, sp;
+    };
+
+    __device__ __forceinline__ void order(Level& lv, const K* Xc, const K* Yc) const {
+        lv.larger = lv.smaller = lv.lp = lv.sp = 0;
+        if (lv.have != 3) return;
+        lv.larger = Xc[batchSize - 1] < Yc[batchSize - 1] ? lv.r : lv.l;
+        lv.smaller = lv.larger == lv.r ? lv.l : lv.r;
+        lv.lp = lv.larger == lv.r ? lv.rPrev : lv.lPrev;
+        lv.sp = lv.larger == lv.r ? lv.lPrev : lv.rPrev;
+    }
+
+    // TD: take the last node; if it is an in-flight insert target, mark it
+    // and wait for the insert to hand its batch over at the root
+    // (heap/tditdd/heap.cuh:371-393).  Thread 0; c->w[7] = 1 when handed over.
+    __device__ __forceinline__ bool takeLastTopDown(int last, OpCtl* c) const {
+        unsigned long long t0 = 0;
+        c->w[7] = 0;
+        for (unsigned it = 0;; ++it) {
+            if (detail::cas_acquire(status + last, TD::AVAIL, TD::INUSE) == TD::AVAIL) return true;
+            if (detail::cas_acquire(status + last, TD::TARGET, TD::MARKED) == TD::TARGET) break;
+            if (!keep_waiting(t0, it, kSiteLockLast, last, detail::ld_relaxed(status + last))) return false;
+        }
+        c->w[7] = 1;
+        t0 = 0;
+        for (unsigned it = 0; detail::cas_acquire(status + last, TD::TARGET, TD::AVAIL) != TD::TARGET; ++it) {
+            if (!keep_waiting(t0, it, kSiteHandOff, last, detail::ld_relaxed(status + last))) return false;
+        }
+        return true;
+    }
+
+    // deleteUpdate body once the root is copied out and batchCount lowered:
+    // take the last node (:355-402), merge it with the partial buffer
+    // (:404-416), release node 0 and the last node, then sift down from the
+    // root.  Locks are taken as late and dropped as early as the protocol
+    // allows: with many blocks in the pipeline, lock hold time is what
+    // bounds throughput (taking the root's children before the partial-buffer
+    // merge, or the next level's children one level ahead, measured slower).
+    __device__ __forceinline__ void refill_and_sift(Op& op, K* base, int last) const {
+        OpCtl* c = op.c;
+        const int tid = threadIdx.x;
+        const int B = batchSize;
+        K* C = base;
+        K* P = base + B;
+        if (tid == 0) {
+            bool ok = true;
+            c->w[7] = 0;
+            if constexpr (VARIANT == kTopDown) {
+                ok = takeLastTopDown(last, c);
             } else {
                 // (:372-378) atomicMax takes the node from AVAIL, INSHOLD or DELMOD
                 unsigned long long t0 = 0;
                 int prev;
-                bool ok = true;
                 for (unsigned it = 0; (prev = detail::max_acquire(status + last, BU::INUSE)) == BU::INUSE; ++it) {
                     if (!keep_waiting(t0, it, kSiteLockLast, last, prev)) { ok = false; break; }
                 }
-                c->abort = !ok;
             }
-            if (!c->abort && last != 1) {
-                op.expect((PB ? 2u : 1u) * nodeBytes());
-                detail::bulk_g2s(s0, node(c->w1 ? 1 : last), nodeBytes(), &c->bar);
-                if (PB) detail::bulk_g2s(s1, node(0), nodeBytes(), &c->bar);
+            if (ok) {
+                op.issue((PB ? 2u : 1u) * nodeBytes());
+                load(C, c->w[7] ? 1 : last, &c->bar);
+                if (PB) load(P, 0, &c->bar);
             }
+            c->abort = !ok;
         }
         __syncthreads();
-        const int last = c->w0;
-        if (last == 1 || c->abort) return;
+        if (c->abort) return;
+        const int lastTaken = !c->w[7];
         if (!op.wait()) return;
-        if (!c->w1) {
-            fill_node(last, B);  // reset the taken node (:396)
-            __syncthreads();
-            if (tid == 0) unlock(last, 0);
+        if (lastTaken) fill_node(last, B);  // reset the taken node (:396)
+        if (PB) merge(C, P, C, node(0));
+        __syncthreads();
+        if (tid == 0) {
+            fence();
+            if (lastTaken) setState(last, 0);
+            setState(0, 0);
         }
-        if constexpr (PB) {  // merge with the partial buffer (:404-416)
-            detail::merge_split<K, IPT>(s0, s1, s0, node(0), B);
-            __syncthreads();
-        }
-        if (tid == 0) unlock(0, 0);
-
-        if constexpr (VARIANT == kTopDown) sift_topdown(op, s0, s1, s2);
-        else sift_bottomup(op, s0, s1, s2);
+        sift_loop(op, 1, 0, C, base + 2 * B, base + 3 * B);
     }
 
-    // Top-down sift from the root (heap/tditdd/heap.cuh:418-532).  s0 holds
-    // the batch being sifted; node `cur` is locked.
-    __device__ __forceinline__ void sift_topdown(Op& op, K* s0, K* s1, K* s2) const {
+    // Sift down from `cur` (held; curPrev = the state it returns to) with the
+    // carried batch in C (heap/tditdd/heap.cuh:418-532, heap/buitdd/heap.cuh:
+    // 403-480).  Per level: the two lock warps take the children at once,
+    // one bulk transaction loads them, the children merge writes the larger
+    // half straight to the larger child, the case analysis against C writes
+    // the current node, and one fence releases both (a second fence to free
+    // the larger child before the case analysis measured slower).
+    __device__ __forceinline__ void sift_loop(Op& op, int cur, int curPrev, K* C, K* Xc, K* Yc) const {
         OpCtl* c = op.c;
         const int tid = threadIdx.x;
         const int B = batchSize;
-        int cur = 1;
         for (;;) {
-            const int l = cur << 1, r = l + 1;
-            if (tid == 0) {
-                // A child counts when its word can be locked from AVAIL; insert
-                // targets (TARGET/MARKED) do not (:425-446).  Unlike the
-                // reference, a TARGET left child does not hide an existing right
-                // child: that right child's keys may be below the new content.
-                bool ok = true;
-                int have = 0;
-                const int kids[2] = {l, r};
-                for (int q = 0; q < 2 && ok; ++q) {
-                    const int x = kids[q];
-                    if (x > batchNum) continue;
-                    unsigned long long t0 = 0;
-                    for (unsigned it = 0;; ++it) {
-                        const int v = detail::ld_relaxed(status + x);
-                        if (v == TD::AVAIL) {
-                            if (detail::cas_acquire(status + x, TD::AVAIL, TD::INUSE) == TD::AVAIL) { have |= 1 << q; break; }
-                        } else if (v != TD::INUSE) {
-                            break;  // an insert target: not a child yet
-                        }
-                        if (!keep_waiting(t0, it, kSiteLockChild, x, v)) { ok = false; break; }
-                    }
-                }
-                c->abort = !ok;
-                c->w0 = have;
-                if (ok && have) {
-                    op.expect((have == 3 ? 2u : 1u) * nodeBytes());
-                    if (have & 1) detail::bulk_g2s(s1, node(l), nodeBytes(), &c->bar);
-                    if (have & 2) detail::bulk_g2s(have == 3 ? s2 : s1, node(r), nodeBytes(), &c->bar);
-                }
-            }
+            Level lv;
+            lv.l = leftOf(cur);
+            lv.r = rightOrNone(lv.l);
+            if (tid == lockThread(0)) { int p; c->w[3] = takeChild(lv.l, p); c->w[4] = p; }
+            if (tid == lockThread(1)) { int p; c->w[5] = takeChild(lv.r, p); c->w[6] = p; }
             __syncthreads();
-            if (c->abort) return;
-            const int have = c->w0;
-            if (have == 0) {  // no children (:452-460)
-                store_node(cur, s0);
-                __syncthreads();
-                if (tid == 0) unlock(cur, TD::AVAIL);
-                return;
+            if (c->w[3] < 0 || c->w[5] < 0) return;
+            lv.have = (c->w[3] == kHeld ? 1 : 0) | (c->w[5] == kHeld ? 2 : 0);
+            lv.lPrev = c->w[4];
+            lv.rPrev = c->w[6];
+            if (tid == 0 && lv.have) {
+                op.issue(((lv.have & 1) + (lv.have >> 1)) * nodeBytes());
+                if (lv.have & 1) load(Xc, lv.l, &c->bar);
+                if (lv.have & 2) load(Yc, lv.r, &c->bar);
             }
             if (!op.wait()) return;
-            if (have != 3) {  // one child (:461-477)
-                const int x = have == 1 ? l : r;
-                detail::merge_split<K, IPT>(s0, s1, node(cur), node(x), B);
+            order(lv, Xc, Yc);
+            if (lv.have == 3) {
+                merge(Xc, Yc, Xc, node(lv.larger));
                 __syncthreads();
-                if (tid == 0) { unlock(cur, TD::AVAIL); unlock(x, TD::AVAIL); }
-                return;
             }
-            // two children (:479-531)
-            const int larger = s1[B - 1] < s2[B - 1] ? r : l;
-            const int smaller = larger == r ? l : r;
-            detail::merge_split<K, IPT>(s1, s2, s1, node(larger), B);
-            __syncthreads();
-            if (tid == 0) unlock(larger, TD::AVAIL);
-            if (s0[0] >= s1[B - 1]) {
-                store_node(cur, s1);
-            } else if (s0[B - 1] <= s1[0]) {
-                store_node(cur, s0);
-                store_node(smaller, s1);
-                __syncthreads();
-                if (tid == 0) { unlock(cur, TD::AVAIL); unlock(smaller, TD::AVAIL); }
-                return;
+            // case analysis against the carried batch
+            int done = 1, single = 0;
+            if (lv.have == 0) {  // no children (:452-460)
+                store_node(cur, C);
+            } else if (lv.have != 3) {  // one child (:461-477)
+                single = lv.have == 1 ? lv.l : lv.r;
+                merge(C, lv.have == 1 ? Xc : Yc, node(cur), node(single));
+            } else if (C[0] >= Xc[B - 1]) {
+                store_node(cur, Xc);  // the carried batch goes on unchanged
+                done = 0;
+            } else if (VARIANT == kTopDown ? (C[B - 1] <= Xc[0]) : (C[B - 1] < Xc[0])) {
+                store_node(cur, C);
+                store_node(lv.smaller, Xc);
             } else {
-                detail::merge_split<K, IPT>(s0, s1, node(cur), s0, B);
+                merge(C, Xc, node(cur), C);
+                done = 0;
             }
             __syncthreads();
-            if (tid == 0) unlock(cur, TD::AVAIL);
-            cur = smaller;
-        }
-    }
-
-    // Bottom-up-layout sift from the root (heap/buitdd/heap.cuh:403-480).
-    __device__ __forceinline__ void sift_bottomup(Op& op, K* s0, K* s1, K* s2) const {
-        OpCtl* c = op.c;
-        const int tid = threadIdx.x;
-        const int B = batchSize;
-        int cur = 1, curPrev = BU::AVAIL;
-        for (;;) {
-            const int l = leftOf(cur);
-            const int r = l <= batchNum ? rightOf(l) : batchNum + 1;
             if (tid == 0) {
-                // (:409-418) atomicMax takes a child from AVAIL, INSHOLD or
-                // DELMOD; a child held INSHOLD by a bubbling insert is handed
-                // back as DELMOD.
-                bool ok = true;
-                int prevs[2] = {BU::AVAIL, BU::AVAIL};
-                const int kids[2] = {l, r};
-                int have = 0;
-                for (int q = 0; q < 2 && ok; ++q) {
-                    const int x = kids[q];
-                    if (x > batchNum) continue;
-                    unsigned long long t0 = 0;
-                    int prev;
-                    for (unsigned it = 0; (prev = detail::max_acquire(status + x, BU::INUSE)) == BU::INUSE; ++it) {
-                        if (!keep_waiting(t0, it, kSiteLockChild, x, prev)) { ok = false; break; }
-                    }
-                    if (ok) { have |= 1 << q; prevs[q] = prev == BU::INSHOLD ? BU::DELMOD : prev; }
-                }
-                c->abort = !ok;
-                c->w0 = have;
-                c->w1 = prevs[0];
-                c->w2 = prevs[1];
-                if (ok && have) {
-                    op.expect((have == 3 ? 2u : 1u) * nodeBytes());
-                    if (have & 1) detail::bulk_g2s(s1, node(l), nodeBytes(), &c->bar);
-                    if (have & 2) detail::bulk_g2s(s2, node(r), nodeBytes(), &c->bar);
-                }
+                fence();
+                if (single) setState(single, single == lv.l ? lv.lPrev : lv.rPrev);
+                if (lv.have == 3) setState(lv.larger, lv.lp);
+                setState(cur, curPrev);
+                if (done && lv.have == 3) setState(lv.smaller, lv.sp);
             }
-            __syncthreads();
-            if (c->abort) return;
-            const int have = c->w0, lPrev = c->w1, rPrev = c->w2;
-            if (have == 0) {  // no child inside the allocation
-                store_node(cur, s0);
-                __syncthreads();
-                if (tid == 0) unlock(cur, curPrev);
-                return;
-            }
-            if (!op.wait()) return;
-            if (have == 1) {  // only the left child lies inside the allocation
-                detail::merge_split<K, IPT>(s0, s1, node(cur), node(l), B);
-                __syncthreads();
-                if (tid == 0) { unlock(cur, curPrev); unlock(l, lPrev); }
-                return;
-            }
-            const int larger = s1[B - 1] < s2[B - 1] ? r : l;
-            const int largerPrev = larger == r ? rPrev : lPrev;
-            const int smaller = larger == r ? l : r;
-            const int smallerPrev = larger == r ? lPrev : rPrev;
-            detail::merge_split<K, IPT>(s1, s2, s1, node(larger), B);
-            __syncthreads();
-            if (tid == 0) unlock(larger, largerPrev);
-            if (s0[0] >= s1[B - 1]) {
-                store_node(cur, s1);
-            } else if (s0[B - 1] < s1[0]) {
-                store_node(cur, s0);
-                store_node(smaller, s1);
-                __syncthreads();
-                if (tid == 0) { unlock(cur, curPrev); unlock(smaller, smallerPrev); }
-                return;
-            } else {
-                detail::merge_split<K, IPT>(s0, s1, node(cur), s0, B);
-            }
-            __syncthreads();
-            if (tid == 0) unlock(cur, curPrev);
-            cur = smaller;
-            curPrev = smallerPrev;
+            if (done) return;
+            cur = lv.smaller;
+            curPrev = lv.sp;
         }
     }
 

@@ -39,9 +39,9 @@ def test_host_only_calls(ghlib):
     import gpuheap_gb300 as gh
     assert ghlib.gh_status_string(gh.GH_ERR_TIMEOUT) == b"device wait timed out"
     assert ghlib.gh_heap_view_bytes() == 64
-    # 3 * B keys of merge space + 64 bytes of control + 16 of alignment slack
-    assert ghlib.gh_heap_smem_bytes(0, 1024) == 3 * 1024 * 4 + 80
-    assert ghlib.gh_heap_smem_bytes(2, 1024) == 3 * 1024 * 8 + 80
+    # 4 node buffers of B keys + 128 bytes of control + 16 of alignment slack
+    assert ghlib.gh_heap_smem_bytes(0, 1024) == 4 * 1024 * 4 + 144
+    assert ghlib.gh_heap_smem_bytes(2, 1024) == 4 * 1024 * 8 + 144
 
 
 def test_rejects_bad_arguments_before_touching_a_device(ghlib):

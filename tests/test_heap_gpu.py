@@ -158,6 +158,13 @@ def test_heap_sort_grid(variant, pb, B, logn):
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("B", [2048, 4096])
+def test_heap_sort_large_batches(variant, B):
+    got, want = run_heap_sort("u32", variant, True, B, 1 << 21, seed=B + 5)
+    assert np.array_equal(got, want)
+
+
 @pytest.mark.parametrize("key", ["u64", "i32"])
 @pytest.mark.parametrize("variant", ["topdown", "bottomup"])
 def test_heap_sort_key_types(key, variant):
