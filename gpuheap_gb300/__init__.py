@@ -53,6 +53,7 @@ _SIGS = {
     "gh_heap_snapshot": (_I, [_VP, _VP, _VP, _VP]),
     "gh_heap_inject_lock": (_I, [_VP, _I, _I]),
     "gh_launch_count": (_LL, []),
+    "gh_sort_noalloc": (_I, [_I, _I, _I, _I, _VP, _LL, _VP, _VP]),
     "gh_heap_view_bytes": (ctypes.c_size_t, []),
     "gh_heap_device_view": (_I, [_VP, _VP, ctypes.c_size_t]),
     "gh_heap_smem_bytes": (ctypes.c_size_t, [_I, _I]),

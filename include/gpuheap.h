@@ -122,6 +122,26 @@ gh_status gh_heap_device_view(gh_heap* h, void* view_out, size_t view_bytes);
  * (4 * batch_size keys of node buffers plus 144 bytes of control). */
 size_t gh_heap_smem_bytes(int key_kind, int batch_size);
 
+/* The plain heap-sort of gh_heap_sort for callers that cannot allocate device
+ * memory when they sort: code running under a framework whose caching
+ * allocator already holds the GPU's memory, or latency-critical code that
+ * cannot pay the implicit device synchronization of cudaMalloc/cudaFree.  No
+ * counterpart in the reference (its Heap<K> constructor always cudaMallocs).
+ * It allocates nothing: the heap lives in a fixed 16 MiB array of device
+ * memory inside this library (reserved on every GPU that loads the library,
+ * until the process exits); only in_dev and out_dev come from the caller.
+ * Limit: the heap needs ((ceil(n / batch_size) + 1) * batch_size * key bytes,
+ * rounded up to 256) + (4 * (ceil(n / batch_size) + 2), rounded up to 256) +
+ * 256 bytes <= 16 MiB, e.g. about 4.1 M u32 keys at batch_size 1024; larger
+ * n returns GH_ERR_CAPACITY and prints the sizes.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  Every call reuses the same
+ * array (cleared at the start of each call), so calls whose work overlaps
+ * on the GPU -- other streams, other host threads -- race: serialize them.
+ * Synchronizes `stream` to check the result. */
+gh_status gh_sort_noalloc(int key_kind, int variant, int partial_buffer, int batch_size, const void* in_dev,
+                          long long n, void* out_dev, void* stream);
+
 /* Number of kernels this library has launched since it was loaded. */
 long long gh_launch_count(void);
 
