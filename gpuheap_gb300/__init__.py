@@ -54,6 +54,7 @@ _SIGS = {
     "gh_heap_inject_lock": (_I, [_VP, _I, _I]),
     "gh_launch_count": (_LL, []),
     "gh_sort_noalloc": (_I, [_I, _I, _I, _I, _VP, _LL, _VP, _VP]),
+    "gh_gen_keys": (_I, [_I, _I, ctypes.c_ulonglong, _LL, _VP, _VP]),
     "gh_heap_view_bytes": (ctypes.c_size_t, []),
     "gh_heap_device_view": (_I, [_VP, _VP, ctypes.c_size_t]),
     "gh_heap_smem_bytes": (ctypes.c_size_t, [_I, _I]),
@@ -84,6 +85,36 @@ def lib():
             fn.argtypes = args
         _lib = so
     return _lib
+
+
+def gen_keys(key, seed, dist, n, device="cuda"):
+    """Seeded keys of the plain heap-sort workload on the device (gh_gen_keys):
+    uniform / zipf made there; sorted and reverse are uniform keys sorted in
+    key order.  Returns a torch tensor of the key's width (int32 / int64 bits)."""
+    import torch
+    dt = torch.int64 if key == "u64" else torch.int32
+    out = torch.empty(int(n), dtype=dt, device=device)
+    st = lib().gh_gen_keys(KEY_KINDS[key], 1 if dist == "zipf" else 0, int(seed), int(n), out.data_ptr(),
+                           torch.cuda.current_stream().cuda_stream)
+    _check(st, "gen_keys")
+    if dist in ("sorted", "reverse"):
+        out = sort_keys(out, key)
+        if dist == "reverse":
+            out = out.flip(0)
+    elif dist not in ("uniform", "zipf"):
+        raise ValueError(f"unknown distribution {dist}")
+    return out
+
+
+def sort_keys(t, key):
+    """Key-order sort of a tensor holding key bits (torch; for checks and inputs)."""
+    import torch
+    if key == "i32":
+        return torch.sort(t).values
+    if key == "u32":
+        return torch.sort(t.to(torch.int64) & 0xFFFFFFFF).values.to(torch.int32)
+    flip = torch.tensor(-(2**63), dtype=torch.int64, device=t.device)
+    return torch.sort(t ^ flip).values ^ flip
 
 
 def launch_count():

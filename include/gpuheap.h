@@ -142,6 +142,15 @@ size_t gh_heap_smem_bytes(int key_kind, int batch_size);
 gh_status gh_sort_noalloc(int key_kind, int variant, int partial_buffer, int batch_size, const void* in_dev,
                           long long n, void* out_dev, void* stream);
 
+/* Seeded synthetic keys for the plain heap-sort workload, made on the device:
+ * key i depends only on (seed, i) (splitmix64 finaliser on seed + (i+1) *
+ * 0x9e3779b97f4a7c15).  zipf = 0: u32 keys uniform in [0, 2^32 - 2];
+ * zipf = 1: Zipf(1.2) over 2^16 distinct values.  u64 keys are
+ * (u32 key << 32) | i, i32 keys u32 key - 2^31.  Stands in for the
+ * reference drivers' rand() keys (test/heap_test.cu:114-119,
+ * artifacts/synthetic/sort.cu:108-119). */
+gh_status gh_gen_keys(int key_kind, int zipf, unsigned long long seed, long long n, void* out_dev, void* stream);
+
 /* Number of kernels this library has launched since it was loaded. */
 long long gh_launch_count(void);
 

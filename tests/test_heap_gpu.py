@@ -264,3 +264,13 @@ def test_invalid_arguments():
     with pytest.raises(gh.HeapError):
         h.insertion(empty_dev(512, "u32"), 300)  # size > batch_size
     h.close()
+
+
+@pytest.mark.parametrize("key", ["u32", "u64", "i32"])
+@pytest.mark.parametrize("dist", ["uniform", "sorted", "reverse", "zipf"])
+def test_device_key_generator_matches_oracle(key, dist):
+    """The benchmark's device-side workload generator (gh_gen_keys) makes the
+    oracle's keys bit for bit."""
+    n = (1 << 18) + 17
+    got = to_host(gh.gen_keys(key, 1234, dist, n), key)
+    assert np.array_equal(got, pyoracle.gen(key, 1234, dist, n))
