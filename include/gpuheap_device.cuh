@@ -556,14 +556,16 @@ struct Heap {
             if (ok) {
                 c->bc = detail::ld_relaxed(&state->batchCount);
                 c->ps = detail::ld_relaxed(&state->partialBufferSize);
-                if (PB) { op.issue(nodeBytes()); load(s1, 0, &c->bar); }
+                // a full batch meeting an empty partial buffer merges with
+                // padding only: that merge (case 2.2) changes nothing, skip it
+                if (PB && !(c->ps == 0 && size == batchSize)) { op.issue(nodeBytes()); load(s1, 0, &c->bar); }
             }
         }
         __syncthreads();
         if (c->abort) return;
         const int bc = c->bc, ps = c->ps;
 
-        if constexpr (PB) {
+        if constexpr (PB) if (!(ps == 0 && size == B)) {
             if (!op.wait()) return;
             if (bc == 0 && size < B) {
                 if (ps == 0) {  // case 1.1 (:575-584)
@@ -876,6 +878,7 @@ struct Heap {
         OpCtl* c = op.c;
         if (threadIdx.x == 0) {
             const int last = detail::ld_relaxed(&state->batchCount);
+            c->ps = detail::ld_relaxed(&state->partialBufferSize);
             detail::st_relaxed(&state->batchCount, last - 1);
             c->w[0] = last;
         }
@@ -934,6 +937,9 @@ struct Heap {
         const int B = batchSize;
         K* C = base;
         K* P = base + B;
+        // an empty partial buffer is all padding: merging with it (:404-416)
+        // changes nothing, so it is neither loaded nor merged
+        const bool pb = PB && c->ps != 0;
         if (tid == 0) {
             bool ok = true;
             c->w[7] = 0;
@@ -948,9 +954,9 @@ struct Heap {
                 }
             }
             if (ok) {
-                op.issue((PB ? 2u : 1u) * nodeBytes());
+                op.issue((pb ? 2u : 1u) * nodeBytes());
                 load(C, c->w[7] ? 1 : last, &c->bar);
-                if (PB) load(P, 0, &c->bar);
+                if (pb) load(P, 0, &c->bar);
             }
             c->abort = !ok;
         }
@@ -959,7 +965,7 @@ struct Heap {
         const int lastTaken = !c->w[7];
         if (!op.wait()) return;
         if (lastTaken) fill_node(last, B);  // reset the taken node (:396)
-        if (PB) merge(C, P, C, node(0));
+        if (pb) merge(C, P, C, node(0));
         __syncthreads();
         if (tid == 0) {
             fence();
