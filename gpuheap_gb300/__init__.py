@@ -42,6 +42,7 @@ _SIGS = {
     "gh_heap_set_grid": (_I, [_VP, _I]),
     "gh_heap_insert": (_I, [_VP, _VP, _LL, _I, _VP]),
     "gh_heap_delete": (_I, [_VP, _VP, _LL, ctypes.POINTER(_LL), _VP]),
+    "gh_heap_concurrent": (_I, [_VP, _VP, _LL, _I, _VP, _LL, ctypes.POINTER(_LL), _VP]),
     "gh_heap_sync": (_I, [_VP, _VP]),
     "gh_heap_insert_batch": (_I, [_VP, _VP, _I, _VP]),
     "gh_heap_delete_batch": (_I, [_VP, _VP, ctypes.POINTER(_I), _VP]),
@@ -55,6 +56,9 @@ _SIGS = {
     "gh_launch_count": (_LL, []),
     "gh_sort_noalloc": (_I, [_I, _I, _I, _I, _VP, _LL, _VP, _VP]),
     "gh_gen_keys": (_I, [_I, _I, ctypes.c_ulonglong, _LL, _VP, _VP]),
+    "gh_rmat_edges": (_I, [_I, _LL, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong,
+                           ctypes.c_uint, _VP, _VP, _VP, _VP]),
+    "gh_sssp": (_I, [_VP, _I, _VP, _VP, _VP, _I, _VP, _VP, ctypes.POINTER(ctypes.c_ulonglong)]),
     "gh_heap_view_bytes": (ctypes.c_size_t, []),
     "gh_heap_device_view": (_I, [_VP, _VP, ctypes.c_size_t]),
     "gh_heap_smem_bytes": (ctypes.c_size_t, [_I, _I]),
@@ -252,6 +256,17 @@ class Heap:
             return None
         got = _LL()
         _check(lib().gh_heap_delete(self._h, _ptr(out), max_keys, ctypes.byref(got), _stream(stream)), "delete")
+        return got.value
+
+    def concurrent(self, keys, out, n=None, chunk=0, max_keys=None, stream=None):
+        """concurrentKernel (test/heap_test.cu:13-38): half the grid inserts
+        keys[0, n) while the other half makes n // batch_size deletes into
+        out; returns the number of keys deleted."""
+        n = keys.numel() if n is None else int(n)
+        max_keys = out.numel() if max_keys is None else int(max_keys)
+        got = _LL()
+        _check(lib().gh_heap_concurrent(self._h, _ptr(keys), n, int(chunk), _ptr(out), max_keys, ctypes.byref(got),
+                                        _stream(stream)), "concurrent")
         return got.value
 
     def sort(self, keys, out, n=None, stream=None):

@@ -205,7 +205,9 @@ gh_status gh_heap_reset(gh_heap* h, void* stream) {
 }
 
 gh_status gh_heap_set_timeout(gh_heap* h, double seconds) {
-    if (!h || !(seconds > 0)) return GH_ERR_INVALID;
+    // at most 60 s: a bottom-up park (two waits) must end before 2^29 later
+    // inserts could reuse its ticket
+    if (!h || !(seconds > 0) || seconds > 60.0) return GH_ERR_INVALID;
     h->d.timeoutNs = static_cast<long long>(seconds * 1e9);
     return GH_OK;
 }
@@ -265,6 +267,37 @@ gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long lon
         return device_error(h);
     }
     return GH_OK;
+}
+
+gh_status gh_heap_concurrent(gh_heap* h, const void* keys_dev, long long n, int chunk, void* out_dev,
+                             long long max_keys, long long* n_out, void* stream) {
+    if (!h || n < 0 || (n > 0 && !keys_dev) || max_keys < 0 || (max_keys > 0 && !out_dev)) return GH_ERR_INVALID;
+    if (chunk == 0) chunk = h->d.batchSize;
+    if (chunk < 1 || chunk > h->d.batchSize) return GH_ERR_INVALID;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    gh::impl::LaunchArgs a = args_of(h, s);
+    if (a.grid < 2) a.grid = 2;  // one inserting and one deleting block at least
+    const long long deletes = n / h->d.batchSize;
+    const int lim = static_cast<int>(std::min<long long>(max_keys, INT_MAX));
+    gh::impl::k_set_output<<<1, 32, 0, s>>>(h->d.state, 0, lim);
+    gh::impl::count_launch();
+    GH_CUDA(cudaGetLastError());
+    if (n > 0) {
+        gh_status st = with_key(h, [&](auto k) {
+            using K = decltype(k);
+            return gh::impl::launch_concurrent<K>(a, static_cast<const K*>(keys_dev), n, chunk, static_cast<K*>(out_dev),
+                                                  max_keys > 0 ? deletes : 0);
+        });
+        if (st != GH_OK) return st;
+    }
+    gh::impl::k_set_output<<<1, 32, 0, s>>>(h->d.state, -1, INT_MAX);
+    gh::impl::count_launch();
+    GH_CUDA(cudaGetLastError());
+    int dc = 0;
+    GH_CUDA(cudaMemcpyAsync(&dc, &h->d.state->deleteCount, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GH_CUDA(cudaStreamSynchronize(s));
+    if (n_out) *n_out = dc;
+    return device_error(h);
 }
 
 gh_status gh_heap_insert_batch(gh_heap* h, const void* keys_dev, int size, void* stream) {

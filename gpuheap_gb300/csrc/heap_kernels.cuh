@@ -60,6 +60,30 @@ __global__ void __launch_bounds__(1024) k_delete(H h, K* out) {
     while (delete_one(h, out) != 0) {}
 }
 
+// concurrentKernel (test/heap_test.cu:13-38): the first half of the grid
+// inserts keys[0, n) in chunks of `chunk`, the second half makes
+// `deletes` deleteRoot/deleteUpdate attempts, both grid-strided over their
+// half, all at the same time.  An attempt on an empty heap writes nothing.
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_concurrent(H h, const K* __restrict__ keys, long long n, int chunk,
+                                                     K* out, long long deletes) {
+    const int half = gridDim.x / 2;
+    if (static_cast<int>(blockIdx.x) < half) {
+        const long long nchunks = (n + chunk - 1) / chunk;
+        for (long long i = blockIdx.x; i < nchunks; i += half) {
+            const long long off = i * chunk;
+            const long long rem = n - off;
+            h.insertion(keys + off, rem < chunk ? static_cast<int>(rem) : chunk, 0);
+            if (h.failed()) return;
+        }
+    } else {
+        for (long long i = blockIdx.x - half; i < deletes; i += gridDim.x - half) {
+            delete_one(h, out);
+            if (h.failed()) return;
+        }
+    }
+}
+
 // One delete by one block; the size goes to *sizeOut.
 template <typename H, typename K>
 __global__ void __launch_bounds__(1024) k_delete_one(H h, K* out, int* sizeOut) {
@@ -79,10 +103,13 @@ static __global__ void k_init_state(HeapState* st, int deleteCount) {
         st->partialBufferSize = 0;
         st->deleteCount = deleteCount;
         st->outLimit = INT_MAX;
+        st->insTicket = 0;
         st->err = 0;
         st->errOp = 0;
         st->errNode = 0;
         st->errState = 0;
+        st->busy = 0;
+        for (int q = 0; q < 8; ++q) st->appStats[q] = 0;
     }
 }
 

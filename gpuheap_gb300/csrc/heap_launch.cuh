@@ -24,6 +24,8 @@ template <typename K>
 cudaError_t launch_erase(const LaunchArgs& a, K* out);
 template <typename K>
 cudaError_t launch_erase_one(const LaunchArgs& a, K* out);
+template <typename K>
+cudaError_t launch_concurrent(const LaunchArgs& a, const K* keys, long long n, int chunk, K* out, long long deletes);
 // Bytes of gh::Heap<K, variant, pb> (IPT chosen at run time) for application kernels.
 template <typename K>
 void device_view(const Desc& d, void* out, size_t* bytes);
@@ -103,6 +105,20 @@ cudaError_t launch_erase(const LaunchArgs& a, K* out) {
 }
 
 template <typename K>
+cudaError_t launch_concurrent(const LaunchArgs& a, const K* keys, long long n, int chunk, K* out, long long deletes) {
+    return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
+        using H = decltype(proto);
+        const H h = view_of<H>(*a.d, 1);
+        const size_t smem = H::smemBytes(a.d->batchSize);
+        cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_concurrent<H, K>), smem);
+        if (e != cudaSuccess) return e;
+        k_concurrent<H, K><<<a.grid, a.threads, smem, a.stream>>>(h, keys, n, chunk, out, deletes);
+        count_launch();
+        return cudaGetLastError();
+    });
+}
+
+template <typename K>
 cudaError_t launch_erase_one(const LaunchArgs& a, K* out) {
     return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
         using H = decltype(proto);
@@ -132,6 +148,7 @@ void device_view(const Desc& d, void* out, size_t* bytes) {
     template cudaError_t launch_insert<K>(const LaunchArgs&, const K*, long long, int);          \
     template cudaError_t launch_erase<K>(const LaunchArgs&, K*);                                 \
     template cudaError_t launch_erase_one<K>(const LaunchArgs&, K*);                             \
+    template cudaError_t launch_concurrent<K>(const LaunchArgs&, const K*, long long, int, K*, long long); \
     template void device_view<K>(const Desc&, void*, size_t*);
 #endif  // GH_INSTANTIATE
 

@@ -49,7 +49,7 @@ gh_status gh_heap_destroy(gh_heap* h);
 /* reset(): heap/tditdd/heap.cuh:69-91 (also clears a recorded device error). */
 gh_status gh_heap_reset(gh_heap* h, void* stream);
 
-/* Time limit of every device-side wait (default 2 s). */
+/* Time limit of every device-side wait, in (0, 60] seconds (default 2 s). */
 gh_status gh_heap_set_timeout(gh_heap* h, double seconds);
 /* Threads per block for the bulk entry points (0 = automatic: 16-byte merge
  * runs per thread); a power of two in [32, 1024] with 2*batch_size/threads
@@ -68,6 +68,17 @@ gh_status gh_heap_insert(gh_heap* h, const void* keys_dev, long long n, int chun
  * are written in ascending order (HEAP_SORT) to out_dev[0, *n_out).  When
  * n_out is not NULL the call synchronizes the stream to read the count. */
 gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long long* n_out, void* stream);
+
+/* concurrentKernel (test/heap_test.cu:13-38, test/partial_heap_test.cu:13-38):
+ * one launch in which the first half of the grid inserts keys_dev[0, n) in
+ * insertion() calls of `chunk` keys (0 = batch_size) while the second half
+ * makes n / batch_size deleteRoot/deleteUpdate attempts (an attempt on an
+ * empty heap writes nothing).  Deleted keys go to out_dev[0, *n_out) one
+ * batch after another (each batch ascending; batches in the order their
+ * deletes took the root), at most max_keys of them.  The grid is at least 2
+ * blocks.  Synchronizes the stream. */
+gh_status gh_heap_concurrent(gh_heap* h, const void* keys_dev, long long n, int chunk, void* out_dev,
+                             long long max_keys, long long* n_out, void* stream);
 
 /* Waits for the stream and reports the first error the heap recorded on the
  * device (the bulk entry points above return before their kernels finish). */
@@ -150,6 +161,26 @@ gh_status gh_sort_noalloc(int key_kind, int variant, int partial_buffer, int bat
  * reference drivers' rand() keys (test/heap_test.cu:114-119,
  * artifacts/synthetic/sort.cu:108-119). */
 gh_status gh_gen_keys(int key_kind, int zipf, unsigned long long seed, long long n, void* out_dev, void* stream);
+
+/* R-MAT edges (Chakrabarti et al. 2004): edge e gets `scale` quadrant choices
+ * with probabilities a, b, c, 1-a-b-c from counter-based draws on (seed, e),
+ * and a weight uniform in [1, max_weight].  Device outputs of m entries.
+ * Stands in for the reference's graph files (applications/sssp_longfei_new/
+ * main.cu:24-61, which are not in the repository). */
+gh_status gh_rmat_edges(int scale, long long m, double a, double b, double c, unsigned long long seed,
+                        unsigned max_weight, int* src_dev, int* dst_dev, unsigned* w_dev, void* stream);
+
+/* Single-source shortest paths driven by the heap `h` (u64 keys, partial
+ * buffer on, block threads <= batch size): the caller pattern of
+ * applications/sssp_longfei_new/sssp.cu:19-132 (take a batch of
+ * dist << 32 | vertex keys, skip stale ones, relax their edges with
+ * atomicMin, insert the improved keys) on this repository's device API.
+ * CSR graph with n vertices: rowptr_dev (n + 1, int64), col_dev (int32),
+ * w_dev (u32).  dist_dev (n, u32) gets the distances, UINT32_MAX where
+ * unreachable.  The heap is reset first.  Synchronizes; stats_host (may be
+ * NULL) gets {keys taken, edges scanned, keys inserted}. */
+gh_status gh_sssp(gh_heap* h, int n, const long long* rowptr_dev, const int* col_dev, const unsigned* w_dev,
+                  int source, unsigned* dist_dev, void* stream, unsigned long long* stats_host);
 
 /* Number of kernels this library has launched since it was loaded. */
 long long gh_launch_count(void);

@@ -21,8 +21,8 @@
 //   * the insert batch is sorted by a bitonic network whose short strides run
 //     under __syncwarp instead of __syncthreads;
 //   * locks use acquire/release atomics at GPU scope (the reference publishes
-//     node data with plain stores), and node reads after a lock are ordered
-//     by fence.proxy.async before the bulk copy;
+//     node data with plain stores); a bulk copy reads a node only after the
+//     lock acquire that follows its writer's fence.acq_rel.gpu + release;
 //   * every wait is bounded by a time limit; on expiry the block records an
 //     error in HeapState::err and returns, and every other block stops at its
 //     next wait, so a broken heap never hangs the GPU;
@@ -44,7 +44,15 @@ enum Variant : int { kTopDown = 0, kBottomUp = 1 };
 // transition table at :242-258.  Bottom-up heaps: heap/buitdd/heap.cuh:6-9,
 // table at :258-274.
 struct TD { static constexpr int AVAIL = 0, INUSE = 1, TARGET = 2, MARKED = 3; };
-struct BU { static constexpr int AVAIL = 0, INSHOLD = 1, DELMOD = 2, INUSE = 3; };
+// A bottom-up insert parks its node with INSHOLD tagged by a ticket unique
+// among concurrent inserts (kParkBase + ticket), so that on taking the node
+// back it can tell whether anyone else held it meanwhile.  INUSE stays the
+// largest value, so the deleters' atomicMax takes every other state.
+struct BU {
+    static constexpr int AVAIL = 0, INSHOLD = 1, DELMOD = 2, INUSE = 1 << 30;
+    static constexpr int kParkBase = 4, kTicketMask = (1 << 29) - 1;
+    __host__ __device__ static constexpr bool parked(int v) { return v == INSHOLD || (v >= kParkBase && v < INUSE); }
+};
 
 enum DeviceError : int { kErrNone = 0, kErrInvalid = 1, kErrCapacity = 2, kErrTimeout = 3 };
 
@@ -54,7 +62,8 @@ enum ErrSite : int {
     kSiteLockLast = 5, kSiteLockChild = 6, kSiteHandOff = 7, kSiteBulkCopy = 8, kSiteCapacity = 9
 };
 
-// Heap counters and the sticky error record, one 128-byte line each.
+// Heap counters, the sticky error record and application words, one
+// 128-byte line each.
 struct alignas(128) HeapState {
     int batchCount;         // full nodes (reference: *batchCount)
     int partialBufferSize;  // keys held in node 0 (reference: *partialBufferSize)
@@ -66,6 +75,10 @@ struct alignas(128) HeapState {
     int errNode;            // node whose wait failed
     int errState;           // lock word value last seen there
     int pad1[28];
+    int busy;               // applications: blocks between taking a batch and finishing its inserts
+    int insTicket;          // bottom-up inserts: next park ticket (atomicAdd)
+    int pad2[14];
+    unsigned long long appStats[8];  // applications: counters (e.g. pops, expansions, relaxations)
 };
 
 // Per-operation control block at the end of the heap's shared-memory region:
@@ -407,7 +420,7 @@ struct Heap {
             // DELMOD; a node a bubbling insert holds (INSHOLD) goes back as DELMOD.
             const int v = detail::max_acquire(status + x, BU::INUSE);
             if (v == BU::INUSE) return kPending;
-            prev = v == BU::INSHOLD ? BU::DELMOD : v;
+            prev = BU::parked(v) ? BU::DELMOD : v;
             return kHeld;
         }
     }
@@ -542,6 +555,11 @@ struct Heap {
         OpCtl* c = op.c;
         const int B = batchSize;
         const int tid = threadIdx.x;
+        // bottom-up park ticket: drawn now, its latency hidden by the sort
+        int parkTag = 0;
+        if constexpr (VARIANT == kBottomUp) {
+            if (tid == 0) parkTag = BU::kParkBase + (atomicAdd(&state->insTicket, 1) & BU::kTicketMask);
+        }
 
         // stage and pad with init_limits, then sort (:557-562)
         for (int q = tid; q < B; q += blockDim.x) s0[q] = q < size ? items[q] : init_limits;
@@ -634,7 +652,7 @@ struct Heap {
         }
 
         if constexpr (VARIANT == kTopDown) insert_topdown(op, s0, s1, s2, bc);
-        else insert_bottomup(op, s0, s1, s2, bc);
+        else insert_bottomup(op, s0, s1, s2, bc, parkTag);
     }
 
     // Top-down path (heap/tditdd/heap.cuh:666-752).  Entered holding node 0;
@@ -719,10 +737,27 @@ struct Heap {
     // Bottom-up path (heap/buitdd/heap.cuh:616-689).  Entered holding node 0;
     // the carried batch is in s0.  The reference parks its node as INSHOLD
     // before waiting for the parent; here one attempt at the parent comes
-    // first and the park only happens when that attempt fails.  A level whose
-    // parent already ends at or below the batch changes nothing, and neither
-    // would any level above it, so the walk stops there.
-    __device__ __forceinline__ void insert_bottomup(Op& op, K* s0, K* s1, K* s2, int bc) const {
+    // first and the park only happens when that attempt fails.
+    //
+    // A parked node is taken back with atomicMax; finding its own ticket
+    // (parkTag, drawn by thread 0 when the insertion began) there proves
+    // nobody held it meanwhile, so the cached batch is still the node's
+    // content.  Tickets repeat after 2^29 inserts, which take over 170 s
+    // (every insert holds node 0 for at least one ~330 ns L2 atomic); a park
+    // lasts at most two waits of at most 60 s, so no park outlives its ticket.  Anything else (a deleter sifted through it, or took it as the
+    // last node, reset it, and a new insert claimed it and parked there) makes
+    // the node's memory authoritative, as the reference always reads it
+    // (:643-673), and the batch is reloaded.
+    //
+    // Early stop: a level whose parent already ends at or below the batch
+    // changes nothing, and while no one else has held this insert's nodes no
+    // level above it would change either, so the walk stops there.  Once a
+    // deleter has been through a parked node it walks on to the root like the
+    // reference: that deleter merged the insert's small keys into the parent
+    // it wrote, which can leave them below the grandparent, and only this walk
+    // repairs that.  Stopping early in that case left parent/grandparent
+    // inversions behind when inserts and deletes ran concurrently.
+    __device__ __forceinline__ void insert_bottomup(Op& op, K* s0, K* s1, K* s2, int bc, int parkTag) const {
         OpCtl* c = op.c;
         const int tid = threadIdx.x;
         const int B = batchSize;
@@ -743,6 +778,7 @@ struct Heap {
         __syncthreads();
         K* carried = s0;
         K* spare = s2;
+        if (tid == 0) c->w[2] = 0;  // 1 once someone else has held one of this insert's nodes
         while (cur != 1) {
             const int p = parentOf(cur);
             if (tid == 0) {
@@ -751,7 +787,7 @@ struct Heap {
                 if (detail::cas_acquire(status + p, BU::AVAIL, BU::INUSE) != BU::AVAIL) {
                     // park our node so a deleter can pass through it, then wait
                     fence();
-                    setState(cur, BU::INSHOLD);
+                    setState(cur, parkTag);
                     ok = lock(p, BU::AVAIL, BU::INUSE, kSiteLockPath);
                     if (ok) {
                         unsigned long long t0 = 0;
@@ -759,7 +795,8 @@ struct Heap {
                         for (unsigned it = 0; (prev = detail::max_acquire(status + cur, BU::INUSE)) == BU::INUSE; ++it) {
                             if (!keep_waiting(t0, it, kSiteLockPath, cur, prev)) { ok = false; break; }
                         }
-                        reload = ok && prev != BU::INSHOLD;  // a deleter rewrote it meanwhile
+                        reload = ok && prev != parkTag;
+                        if (reload) c->w[2] = 1;
                     }
                 }
                 if (ok) {
@@ -776,8 +813,8 @@ struct Heap {
             if (s1[0] >= carried[B - 1]) {  // whole batch below the parent: swap (:647-661)
                 store_node(p, carried);
                 store_node(cur, s1);
-            } else if (s1[B - 1] <= carried[0]) {
-                done = 1;  // already ordered: nothing changes here or above
+            } else if (s1[B - 1] <= carried[0] && c->w[2] == 0) {
+                done = 1;  // already ordered, nodes never taken by others: nothing changes here or above
             } else {
                 merge(carried, s1, spare, node(cur));
                 __syncthreads();
@@ -1018,7 +1055,7 @@ struct Heap {
             } else if (C[0] >= Xc[B - 1]) {
                 store_node(cur, Xc);  // the carried batch goes on unchanged
                 done = 0;
-            } else if (VARIANT == kTopDown ? (C[B - 1] <= Xc[0]) : (C[B - 1] < Xc[0])) {
+            } else if (VARIANT == kTopDown || !PB ? (C[B - 1] <= Xc[0]) : (C[B - 1] < Xc[0])) {  // buitdd alone uses < (:451)
                 store_node(cur, C);
                 store_node(lv.smaller, Xc);
             } else {

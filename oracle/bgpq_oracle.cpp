@@ -9,7 +9,9 @@
 #include "bgpq_oracle.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <queue>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -287,7 +289,8 @@ struct Model {
             int smaller = larger == r ? l : r;
             std::vector<K> low(B);
             merge(node(l), node(r), low.data(), node(larger));
-            bool stop = variant == 0 ? (sm[B - 1] <= low[0]) : (sm[B - 1] < low[0]);
+            // ties: tditdd :506, tditdd_np :435 and buitdd_np :392 use <=, buitdd :451 uses <
+            bool stop = (variant == 0 || !pb) ? (sm[B - 1] <= low[0]) : (sm[B - 1] < low[0]);
             if (sm[0] >= low[B - 1]) {
                 std::copy(low.begin(), low.end(), node(cur));
             } else if (stop) {
@@ -372,6 +375,42 @@ void gho_model_destroy(void* m) {
     else if (b->kind == 1) delete static_cast<Model<uint64_t>*>(b->m);
     else delete static_cast<Model<int32_t>*>(b->m);
     delete b;
+}
+
+void gho_dijkstra(int n, const int64_t* rowptr, const int32_t* col, const uint32_t* w, int source, uint32_t* dist) {
+    for (int v = 0; v < n; ++v) dist[v] = 0xffffffffu;
+    if (source < 0 || source >= n) return;
+    std::priority_queue<uint64_t, std::vector<uint64_t>, std::greater<uint64_t>> pq;
+    dist[source] = 0;
+    pq.push(static_cast<uint64_t>(source));
+    while (!pq.empty()) {
+        const uint64_t key = pq.top();
+        pq.pop();
+        const uint32_t d = static_cast<uint32_t>(key >> 32);
+        const int v = static_cast<int>(key & 0xffffffffu);
+        if (d != dist[v]) continue;  // stale entry
+        for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e) {
+            const uint64_t nd64 = static_cast<uint64_t>(d) + w[e];
+            const uint32_t nd = nd64 >= 0xffffffffu ? 0xfffffffeu : static_cast<uint32_t>(nd64);
+            const int u = col[e];
+            if (nd < dist[u]) {
+                dist[u] = nd;
+                pq.push((static_cast<uint64_t>(nd) << 32) | static_cast<uint32_t>(u));
+            }
+        }
+    }
+}
+
+void gho_dijkstra_many(int n, const int64_t* rowptr, const int32_t* col, const uint32_t* w, const int32_t* sources,
+                       int k, int threads, uint32_t* dist_out) {
+    std::atomic<int> next{0};
+    auto worker = [&] {
+        for (int i; (i = next.fetch_add(1)) < k;)
+            gho_dijkstra(n, rowptr, col, w, sources[i], dist_out + static_cast<size_t>(i) * n);
+    };
+    std::vector<std::thread> ts;
+    for (int t = 0; t < std::max(1, threads); ++t) ts.emplace_back(worker);
+    for (auto& t : ts) t.join();
 }
 
 // Algorithmic node traffic of one heap-sort of n keys (bytes):

@@ -77,6 +77,16 @@ void gho_model_state_u64(void* m, uint64_t* items, int* counters);
 void gho_model_state_i32(void* m, int32_t* items, int* counters);
 void gho_model_destroy(void* m);
 
+/* Single-source shortest paths with std::priority_queue on (dist << 32 | v)
+ * keys (the key packing of applications/sssp_longfei_new/sssp.cu:4-6) over a
+ * CSR graph with u32 weights; unreachable vertices get UINT32_MAX.  The
+ * reference ships no CPU SSSP (applications/sssp/main.cpp only parses), so
+ * this is textbook Dijkstra.  *_many runs `k` sources on `threads` host
+ * threads, one source per task; dist_out is k * n. */
+void gho_dijkstra(int n, const int64_t* rowptr, const int32_t* col, const uint32_t* w, int source, uint32_t* dist_out);
+void gho_dijkstra_many(int n, const int64_t* rowptr, const int32_t* col, const uint32_t* w, const int32_t* sources,
+                       int k, int threads, uint32_t* dist_out);
+
 /* Closed-form algorithmic byte count of one heap-sort (bytes moved by the
  * BGPQ node traffic, independent of the implementation). */
 double gho_sort_bytes(uint64_t n, int batch_size, int key_bytes, int partial_buffer);

@@ -41,6 +41,8 @@ def lib():
         so.gho_model_destroy.argtypes = [_VP]
         so.gho_reversed_idx.restype = ctypes.c_uint32
         so.gho_reversed_idx.argtypes = [ctypes.c_uint32]
+        so.gho_dijkstra.argtypes = [ctypes.c_int, _VP, _VP, _VP, ctypes.c_int, _VP]
+        so.gho_dijkstra_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int, _VP]
         so.gho_sort_bytes.restype = ctypes.c_double
         so.gho_sort_bytes.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         _lib = so
@@ -84,6 +86,20 @@ class Result(tuple):
 
 def reversed_idx(i):
     return lib().gho_reversed_idx(i)
+
+
+def dijkstra(rowptr, col, w, sources, threads=1):
+    """CPU Dijkstra (std::priority_queue on dist<<32|v) from each source;
+    returns a (len(sources), n) uint32 array, UINT32_MAX = unreachable."""
+    rowptr = np.ascontiguousarray(rowptr, np.int64)
+    col = np.ascontiguousarray(col, np.int32)
+    w = np.ascontiguousarray(w, np.uint32)
+    src = np.ascontiguousarray(np.atleast_1d(sources), np.int32)
+    n = rowptr.size - 1
+    out = np.empty((src.size, n), np.uint32)
+    lib().gho_dijkstra_many(n, rowptr.ctypes.data, col.ctypes.data, w.ctypes.data, src.ctypes.data, src.size,
+                            threads, out.ctypes.data)
+    return out
 
 
 def sort_bytes(n, batch_size, key_bytes, partial_buffer):

@@ -32,9 +32,10 @@ VARIANTS = ["tditdd", "tditdd_np", "buitdd", "buitdd_np"]
 VP = ctypes.c_void_p
 
 
-def keys_for(rng, kind, n, split):
+def keys_for(rng, kind, n, split, ties=False):
     """Seeded keys; with split=True the first half lies below the second half
-    (the shape of test/partial_heap_test.cu:114-119)."""
+    (the shape of test/partial_heap_test.cu:114-119); with ties=True they come
+    from about 40 values, so equal keys meet in every comparison."""
     dt = TYPES[kind][0]
     if kind == "u64":
         lo, hi = 0, 2**63
@@ -42,6 +43,8 @@ def keys_for(rng, kind, n, split):
         lo, hi = -(2**31), 2**31 - 1
     else:
         lo, hi = 0, 2**32 - 1
+    if ties:
+        return rng.integers(lo, lo + 40, n, dtype=dt)
     if not split:
         return rng.integers(lo, hi, n, dtype=dt)
     mid = lo + (hi - lo) // 2
@@ -78,7 +81,7 @@ def make_ops(rng, scenario, np_variant, B, n):
             pos += s
             ops.append(0)
         ops += [0] * ((n + B - 1) // B + 2)
-    else:  # mixed
+    else:  # mixed (and ties: the same operation mix)
         pos = 0
         while pos < n:
             if rng.random() < 0.65:
@@ -100,7 +103,7 @@ def main():
     case = 0
     for vi, variant in enumerate(VARIANTS):
         for ki, kind in enumerate(["u32", "u64", "i32"]):
-            for si, scenario in enumerate(["sort", "concurrent", "mixed"]):
+            for si, scenario in enumerate(["sort", "concurrent", "mixed", "ties"]):
                 seed = 1000 + 97 * vi + 13 * ki + si
                 rng = np.random.default_rng(seed)
                 B = [16, 32, 64][(vi + ki + si) % 3]
@@ -114,7 +117,7 @@ def main():
                 while bn * B < 2 * n:
                     bn <<= 1
                 dt, ct, lim = TYPES[kind]
-                keys = keys_for(rng, kind, n, scenario == "concurrent")
+                keys = keys_for(rng, kind, n, scenario == "concurrent", ties=scenario == "ties")
                 ops = make_ops(rng, scenario, np_variant, B, n)
                 f = lambda name, res=ctypes.c_int: _fn(ref, variant, kind, name, res)
                 create = f("create", VP)

@@ -51,3 +51,4 @@ def test_rejects_bad_arguments_before_touching_a_device(ghlib):
     assert ghlib.gh_heap_create(ctypes.byref(h), 0, 5, 1, 16, 128, None) == 1   # variant
     assert ghlib.gh_heap_create(None, 0, 0, 1, 16, 128, None) == 1
     assert ghlib.gh_heap_insert(None, None, 0, 0, None) == 1
+    assert ghlib.gh_heap_concurrent(None, None, 0, 0, None, 0, None, None) == 1

@@ -189,6 +189,35 @@ def test_heap_sort_ragged_sizes(B):
         assert np.array_equal(got, want)
 
 
+# test/heap_test.cu:120-171: insert half, concurrent insert + delete, delete the
+# rest.  Deletes that overlap inserts need not come out in global order, so
+# the bar is: no key lost or duplicated over the three phases, a valid heap
+# after the concurrent phase, and a fully sorted final phase.
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("pb", [True, False])
+@pytest.mark.parametrize("B,logn", [(256, 20), (1024, 21)])
+def test_concurrent_insert_and_delete(variant, pb, B, logn):
+    n = 1 << logn
+    for rep in range(3):
+        keys = pyoracle.gen("u64", 77 + rep + B, "uniform", n)  # unique: (u32 << 32) | index
+        h = gh.Heap(batch_num_for(n, B), B, key="u64", variant=variant, partial_buffer=pb)
+        first, second = to_dev(keys[: n // 2], "u64"), to_dev(keys[n // 2:], "u64")
+        h.insert(first, chunk=B)
+        out1 = empty_dev(n, "u64")
+        got1 = h.concurrent(second, out1, chunk=B if not pb else B // 2 + 3)
+        ok, msg = h.check_insert_heap()
+        assert ok, msg
+        assert h.item_count() == n - got1
+        out2 = empty_dev(n, "u64")
+        got2 = h.delete(out2)
+        assert got1 + got2 == n and h.is_empty()
+        tail = to_host(out2, "u64")[:got2]
+        assert np.all(tail[1:] >= tail[:-1])
+        allout = np.concatenate([to_host(out1, "u64")[:got1], tail])
+        assert np.array_equal(np.sort(allout), np.sort(keys))
+        h.close()
+
+
 def test_sort_entry_point():
     n, B = (1 << 20) + 333, 1024
     keys = pyoracle.gen("u32", 21, "uniform", n)
@@ -261,6 +290,10 @@ def test_invalid_arguments():
     h = gh.Heap(16, 256)
     with pytest.raises(gh.HeapError):
         h.set_block_threads(48)
+    with pytest.raises(gh.HeapError):
+        h.set_timeout(61)  # above the 60 s bound of a wait
+    with pytest.raises(gh.HeapError):
+        h.set_timeout(0)
     with pytest.raises(gh.HeapError):
         h.insertion(empty_dev(512, "u32"), 300)  # size > batch_size
     h.close()

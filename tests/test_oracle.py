@@ -65,9 +65,16 @@ def test_golden_is_a_priority_queue(i):
         assert np.array_equal(out[:c["n"]], np.sort(keys))
 
 
-@pytest.mark.parametrize("i", [0, 7, 19, 30])
-def test_checker_accepts_golden_snapshot_and_catches_planted_mistakes(i):
-    c = golden_cases.case(i)
+def _case_index(variant, key, scenario):
+    return next(m["case"] for m in golden_cases.meta()
+                if (m["variant"], m["key"], m["scenario"]) == (variant, key, scenario))
+
+
+# distinct keys and at least three full nodes: not the "ties" cases
+@pytest.mark.parametrize("which", [("tditdd", "u32", "sort"), ("tditdd", "i32", "concurrent"),
+                                   ("buitdd", "u32", "concurrent"), ("buitdd_np", "u64", "sort")])
+def test_checker_accepts_golden_snapshot_and_catches_planted_mistakes(which):
+    c = golden_cases.case(_case_index(*which))
     variant = "topdown" if c["topdown"] else "bottomup"
     B = c["batch_size"]
     items = c["snap_items"].copy()
