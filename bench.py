@@ -57,7 +57,18 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--timeout", type=float, default=2.0,
                    help="device wait limit in seconds (raise it under a profiler)")
-    return p.parse_args()
+    p.add_argument("--workload", choices=["heapsort", "sssp"], default="heapsort",
+                   help="heapsort: the plain heap-sort line (default); sssp: SSSP with the queue")
+    p.add_argument("--scale", type=int, default=22, help="sssp: R-MAT scale")
+    p.add_argument("--sources", type=int, default=32, help="sssp: seeded random sources (one per step)")
+    p.add_argument("--cpu-sources", type=int, default=16, help="sssp: sources in the CPU Dijkstra sample")
+    args = p.parse_args()
+    if args.workload == "sssp":
+        if args.batch == 2048:
+            args.batch = 1024  # the SSSP default batch
+        if "--steps" not in sys.argv:
+            args.steps = args.sources
+    return args
 
 
 def dist_env():
@@ -383,10 +394,114 @@ def our_arm(args):
     return 0
 
 
+# ------------------------------------------------------------------ SSSP
+SSSP_METRIC = "SSSP ms per source, R-MAT scale {scale} (edge factor 16, weights 1-1000), u64 dist<<32|v keys"
+
+
+def sssp_sources(rowptr, k, seed):
+    import numpy as np
+    deg = np.diff(rowptr)
+    return np.random.default_rng(seed).choice(np.nonzero(deg)[0], size=k, replace=False)
+
+
+def sssp_cpu_leg(host, sources, threads):
+    """CPU Dijkstra (std::priority_queue) of the sample sources: the oracle
+    distances and the single-thread and all-core times."""
+    from oracle import pyoracle
+    t0 = time.perf_counter()
+    one = pyoracle.dijkstra(*host, sources[:1], threads=1)
+    t1 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    alld = pyoracle.dijkstra(*host, sources, threads=threads)
+    tall = time.perf_counter() - t0
+    return alld, one, t1, tall
+
+
+def sssp_arm(args):
+    """One step = single-source shortest paths from one seeded source through
+    gh_sssp (the heap-driven label-correcting kernel); the timed region holds
+    `steps` sources back to back with the graph resident in HBM."""
+    import numpy as np
+    import torch
+
+    import gpuheap_gb300 as gh
+    from gpuheap_gb300 import sssp as gs
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    g = gs.rmat_graph(args.scale, 16, seed=args.seed)
+    torch.cuda.synchronize()
+    host = g.host()
+    srcs = sssp_sources(host[0], max(args.sources, args.steps), args.seed)
+    heap = gs.make_heap(g, batch_size=args.batch, variant=args.variant)
+    if args.grid:
+        heap.set_grid(args.grid)
+    heap.set_timeout(args.timeout)
+    info = heap.info()
+    for i in range(args.warmup):
+        gs.sssp(heap, g, int(srcs[i % len(srcs)]))
+    l0 = gh.launch_count()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    per, keys, edges, dists = [], 0, 0, []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev[0].record()
+        for i in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dist, st = gs.sssp(heap, g, int(srcs[i]))
+            e1.record()
+            e1.synchronize()
+            per.append(e0.elapsed_time(e1))
+            keys += st["keys_taken"]
+            edges += st["edges_scanned"]
+            if i < args.cpu_sources:
+                dists.append(dist.cpu().numpy().view(np.uint32).copy())
+        ev[1].record()
+        torch.cuda.synchronize()
+    total_ms = ev[0].elapsed_time(ev[1])
+    launches = gh.launch_count() - l0
+    per_sorted = sorted(per)
+    value = statistics.mean(per)
+    line = {
+        "metric": SSSP_METRIC.format(scale=args.scale), "value": round(value, 2), "unit": "ms/source",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 2),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"SSSP from {args.steps} seeded sources, R-MAT scale {args.scale}, edge factor 16, "
+                               f"a=0.57 b=0.19 c=0.19, symmetrised, u32 weights 1-1000; "
+                               f"batch_size {args.batch} {args.variant} with partial buffer",
+                   "vertices": g.n, "directed_edges": g.m, "batch_size": args.batch, "variant": args.variant,
+                   "block_threads": info["block_threads"], "grid": info["grid"],
+                   "l2": "graph (CSR) and distances larger than L2", "parallelism": f"replicas x{ws}"},
+        "p50_ms": round(per_sorted[len(per) // 2], 2), "p99_ms": round(per_sorted[min(len(per) - 1, int(0.99 * len(per)))], 2),
+        "edges_per_s": round(g.m * args.steps / (total_ms / 1e3), 1),
+        "scanned_edges_per_source": round(edges / args.steps), "keys_taken_per_source": round(keys / args.steps),
+        "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        k = min(args.cpu_sources, args.steps)
+        want, _, t1, tall = sssp_cpu_leg(host, srcs[:k], threads)
+        exact = all(np.array_equal(dists[i], want[i]) for i in range(k))
+        if not exact:
+            raise SystemExit("bench: SSSP distances differ from CPU Dijkstra")
+        line["exact_vs_dijkstra"] = f"{k} of {k} sources bit-exact"
+        line["cpu_baseline"] = {"value": round(1e3 * t1, 2), "unit": "ms/source", "cores": 1, "kind": "port",
+                                "sample": f"std::priority_queue Dijkstra of 1 source on 1 thread; all {threads} "
+                                          f"cores, one source per thread: {round(1e3 * tall / k, 2)} ms/source "
+                                          f"over {k} sources"}
+    heap.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "sssp":
+        return sssp_arm(args)
     return our_arm(args)
 
 

@@ -63,6 +63,18 @@ _SIGS = {
     "gh_heap_device_view": (_I, [_VP, _VP, ctypes.c_size_t]),
     "gh_heap_smem_bytes": (ctypes.c_size_t, [_I, _I]),
     "gh_heap_info": (_I, [_VP] + [ctypes.POINTER(_I)] * 7),
+    "gh_batch_create": (_I, [ctypes.POINTER(_VP), _I, _I, _I]),
+    "gh_batch_destroy": (_I, [_VP]),
+    "gh_batch_set_timeout": (_I, [_VP, ctypes.c_double]),
+    "gh_batch_set_astar_blocks": (_I, [_VP, _LL, _I]),
+    "gh_batch_add_astar": (_I, [_VP, _I, _I, _VP, ctypes.POINTER(_I)]),
+    "gh_batch_add_knapsack": (_I, [_VP, _I, _VP, _VP, _LL, ctypes.POINTER(_I)]),
+    "gh_batch_build": (_I, [_VP, _VP]),
+    "gh_batch_run": (_I, [_VP, _I, _VP]),
+    "gh_batch_results": (_I, [_VP, _VP, _VP, _VP, _VP]),
+    "gh_batch_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                           ctypes.POINTER(_LL)]),
+    "gh_gen_grid": (_I, [_I, _I, ctypes.c_ulonglong, _I, _VP, _I]),
 }
 
 _lib = None

@@ -18,6 +18,7 @@
 
 #include "gpuheap.h"
 #include "heap_launch.cuh"
+#include "worklist.cuh"
 
 struct gh_heap;  // defined in capi.cu; reached through gh_heap_device_view
 
@@ -93,54 +94,20 @@ __global__ void __launch_bounds__(1024) k_sssp(H heap, const long long* __restri
         __syncthreads();
         heap.insertion(reinterpret_cast<typename H::key_type*>(emit), 1, heapOff);
         __syncthreads();
-        if (tid == 0) { __threadfence(); atomicSub(&st->busy, 1); }
+        gh::app::batch_done(st);
     }
     u64 pops = 0, edges = 0, inserted = 0;
     unsigned long long waitStart = 0;
     int lastBusy = -1;
     for (;;) {
-        // Wait until the heap holds keys; stop once it is empty while no block
-        // is between taking a batch and finishing its inserts.  A waiting
-        // block only reads `busy`, so waiters cannot keep each other alive.
-        if (tid == 0) {
-            int verdict = 0;  // 0: take a batch, 1: stop
-            for (unsigned it = 0;; ++it) {
-                const int bc = gh::detail::ld_relaxed(&st->batchCount);
-                const int ps = gh::detail::ld_relaxed(&st->partialBufferSize);
-                if (bc || ps) break;
-                const int b = atomicAdd(&st->busy, 0);
-                __threadfence();  // the counters below are read after busy
-                if (b == 0 && gh::detail::ld_relaxed(&st->batchCount) == 0 &&
-                    gh::detail::ld_relaxed(&st->partialBufferSize) == 0) { verdict = 1; break; }
-                if (gh::detail::ld_relaxed(&st->err) != 0) { verdict = 1; break; }
-                const unsigned long long now = gh::detail::globaltimer();
-                if (b != lastBusy || waitStart == 0) { lastBusy = b; waitStart = now; }
-                if (now - waitStart > static_cast<unsigned long long>(heap.timeoutNs)) {
-                    heap.raise(gh::kErrTimeout, gh::kSiteLockPartial, 0, b);
-                    verdict = 1;
-                    break;
-                }
-                __nanosleep(200);
-            }
-            if (!verdict) {
-                atomicAdd(&st->busy, 1);
-                __threadfence();  // busy counts this block before it can empty the heap
-            }
-            ctl[2] = verdict;
-        }
-        __syncthreads();
-        const int stop = ctl[2];
-        __syncthreads();
-        if (stop) break;
+        if (gh::app::wait_for_keys(heap, &ctl[2], nullptr, lastBusy, waitStart)) break;
         int size = 0;
         if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size)) heap.deleteUpdate(heapOff);
         if (size == 0) {  // another block took the last keys first
-            if (tid == 0) atomicSub(&st->busy, 1);
-            __syncthreads();
+            gh::app::batch_done(st);
             if (heap.failed()) break;
             continue;
         }
-        lastBusy = -1;
         pops += size;
         // degrees of the keys that are still current (stale keys expand nothing)
         for (int i = tid; i < size; i += T) {
@@ -220,12 +187,8 @@ __global__ void __launch_bounds__(1024) k_sssp(H heap, const long long* __restri
         if (rest > 0) heap.insertion(reinterpret_cast<typename H::key_type*>(emit), rest, heapOff);
         inserted += rest;
         __syncthreads();
-        if (tid == 0) {
-            ctl[1] = 0;
-            __threadfence();
-            atomicSub(&st->busy, 1);
-        }
-        __syncthreads();
+        if (tid == 0) ctl[1] = 0;
+        gh::app::batch_done(st);
         if (heap.failed()) break;
     }
     if (tid == 0) {

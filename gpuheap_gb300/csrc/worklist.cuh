@@ -1,0 +1,74 @@
+// Termination protocol for searches whose blocks share one heap (SSSP, grid
+// A*, knapsack branch-and-bound).
+//
+// A block takes a batch (deleteRoot/deleteUpdate), expands it and inserts
+// what it generates.  HeapState::busy counts the blocks between deciding to
+// take a batch and finishing their inserts.  The search is over when the
+// heap is empty while busy is 0: no block holds keys that could still be
+// inserted.  A block that finds the heap empty only reads busy, so waiting
+// blocks cannot keep each other alive; the block that takes a batch counts
+// itself before it can empty the heap.  The reference's applications stop on
+// a count of active blocks in the same way (applications/sssp_longfei_new/
+// sssp.cu:19-132, artifacts/knapsack/models_pq.cuh:52-137 activeCount).
+#pragma once
+#include "gpuheap_device.cuh"
+
+namespace gh {
+namespace app {
+
+// Thread 0 waits until the heap holds keys (then this block is counted busy
+// and the call returns false: take a batch) or the search is over, `stop`
+// (may be NULL) is set, or the heap has an error (returns true).  Every
+// thread calls it; the result is block-uniform.  `word` is a shared int.
+// A wait with no change of busy for longer than the heap's time limit
+// records a timeout and stops.
+template <typename H>
+__device__ __forceinline__ bool wait_for_keys(const H& heap, int* word, const int* stop, int& lastBusy,
+                                              unsigned long long& waitStart) {
+    HeapState* st = heap.state;
+    if (threadIdx.x == 0) {
+        int verdict = 0;
+        for (;;) {
+            if (stop && detail::ld_relaxed(stop) != 0) { verdict = 1; break; }
+            const int bc = detail::ld_relaxed(&st->batchCount);
+            const int ps = detail::ld_relaxed(&st->partialBufferSize);
+            if (bc || ps) break;
+            const int b = atomicAdd(&st->busy, 0);
+            __threadfence();  // the counters below are read after busy
+            if (b == 0 && detail::ld_relaxed(&st->batchCount) == 0 &&
+                detail::ld_relaxed(&st->partialBufferSize) == 0) { verdict = 1; break; }
+            if (detail::ld_relaxed(&st->err) != 0) { verdict = 1; break; }
+            const unsigned long long now = detail::globaltimer();
+            if (b != lastBusy || waitStart == 0) { lastBusy = b; waitStart = now; }
+            if (now - waitStart > static_cast<unsigned long long>(heap.timeoutNs)) {
+                heap.raise(kErrTimeout, kSiteLockPartial, 0, b);
+                verdict = 1;
+                break;
+            }
+            __nanosleep(200);
+        }
+        if (!verdict) {
+            atomicAdd(&st->busy, 1);
+            __threadfence();  // busy counts this block before it can empty the heap
+        }
+        *word = verdict;
+    }
+    __syncthreads();
+    const bool r = *word != 0;
+    __syncthreads();
+    if (!r) lastBusy = -1;
+    return r;
+}
+
+// The block has inserted everything it generated from its batch.
+__device__ __forceinline__ void batch_done(HeapState* st) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicSub(&st->busy, 1);
+    }
+    __syncthreads();
+}
+
+}  // namespace app
+}  // namespace gh

@@ -182,6 +182,68 @@ gh_status gh_rmat_edges(int scale, long long m, double a, double b, double c, un
 gh_status gh_sssp(gh_heap* h, int n, const long long* rowptr_dev, const int* col_dev, const unsigned* w_dev,
                   int source, unsigned* dist_dev, void* stream, unsigned long long* stats_host);
 
+/* ------------------------------------------------------------------------
+ * Batched searches: many independent grid A* and 0/1 knapsack instances of
+ * uneven size, each with its own heap (u64 keys, partial buffer), run by one
+ * persistent launch.  The reference runs one search per process and launch
+ * (artifacts/astar/main.cu, artifacts/knapsack/main.cu); its per-search
+ * kernels are artifacts/astar/pq_model.cuh:299-371 and
+ * artifacts/knapsack/models_pq.cuh:52-137, whose caller pattern the device
+ * code follows.  A batch is built once (instances uploaded into one device
+ * arena) and can then be run any number of times; each run starts every
+ * search from scratch.
+ * ------------------------------------------------------------------------ */
+typedef struct gh_batch gh_batch;
+typedef enum { GH_SEARCH_ASTAR = 0, GH_SEARCH_KNAPSACK = 1 } gh_search_kind;
+typedef enum { GH_BATCH_PERSISTENT = 0, GH_BATCH_GRAPH = 1, GH_BATCH_PLAIN = 2 } gh_batch_mode;
+
+/* batch_size: power of two in [32, 1024]; block_threads 0 (= min(batch_size,
+ * 512)), batch_size or batch_size / 2, at most 512. */
+gh_status gh_batch_create(gh_batch** out, int batch_size, int variant, int block_threads);
+gh_status gh_batch_destroy(gh_batch* b);
+/* Time limit of every device-side wait, in (0, 60] seconds (default 2 s). */
+gh_status gh_batch_set_timeout(gh_batch* b, double seconds);
+/* A* instances of width * height cells get min(max_blocks,
+ * max(1, cells / cells_per_block)) blocks (default 2^18 cells, 8 blocks);
+ * knapsack instances get one. */
+gh_status gh_batch_set_astar_blocks(gh_batch* b, long long cells_per_block, int max_blocks);
+/* Grid A*: cost_host[y * width + x] in 1..9 is the cost of entering the cell,
+ * 0 an obstacle; the search runs from (0, 0) to (width-1, height-1) with the
+ * Manhattan heuristic (artifacts/astar/astar_map.cuh:137-138 keeps start and
+ * goal free the same way).  Result: the optimal path cost, UINT32_MAX if the
+ * goal is unreachable.  *id (may be NULL) gets the instance index. */
+gh_status gh_batch_add_astar(gh_batch* b, int width, int height, const unsigned char* cost_host, int* id);
+/* 0/1 knapsack with n <= 1024 items (weights >= 1, profits >= 0, total
+ * profit < 2^30): best-first branch-and-bound on the Dantzig bound
+ * (artifacts/knapsack/knapsackKernel.cuh:4-91).  Result: the optimum. */
+gh_status gh_batch_add_knapsack(gh_batch* b, int n, const int* weight_host, const int* profit_host, long long capacity,
+                                int* id);
+/* Lays out one device arena for every instance and uploads them
+ * (synchronizes the stream). */
+gh_status gh_batch_build(gh_batch* b, void* stream);
+/* Runs every search once: GH_BATCH_PERSISTENT one persistent launch over all
+ * instances; GH_BATCH_GRAPH the same replayed from a CUDA graph captured on
+ * the first call; GH_BATCH_PLAIN one launch per instance, back to back (the
+ * reference's way).  Asynchronous. */
+gh_status gh_batch_run(gh_batch* b, int mode, void* stream);
+/* Synchronizes and copies out per-instance results (may be NULL), status
+ * (gh_status per instance, may be NULL) and stats (3 per instance: keys
+ * taken, keys expanded, keys inserted; may be NULL).  Returns the first
+ * instance failure, GH_OK if none. */
+gh_status gh_batch_results(gh_batch* b, long long* results, int* status, unsigned long long* stats, void* stream);
+/* Instances, tasks (block slots), blocks of the persistent launch, block
+ * threads and arena bytes (any pointer may be NULL). */
+gh_status gh_batch_info(gh_batch* b, int* count, int* tasks, int* grid, int* threads, long long* arena_bytes);
+
+/* Seeded synthetic cost grid for grid A* (host memory, `threads` host
+ * threads): cell i draws r = splitmix64(seed + (i + 1) * golden ratio); it is
+ * an obstacle (0) when (r >> 32) % 1000 < obstacle_per_mille, else its cost
+ * is 1 + (r mod 2^32) % 9; the start and goal cells are never obstacles
+ * (artifacts/astar/astar_map.cuh:137-138).  Stands in for the reference's
+ * map files, which are not in the repository. */
+gh_status gh_gen_grid(int width, int height, unsigned long long seed, int obstacle_per_mille, unsigned char* out_host,
+                      int threads);
+
 /* Number of kernels this library has launched since it was loaded. */
 long long gh_launch_count(void);
 

@@ -87,6 +87,24 @@ void gho_dijkstra(int n, const int64_t* rowptr, const int32_t* col, const uint32
 void gho_dijkstra_many(int n, const int64_t* rowptr, const int32_t* col, const uint32_t* w, const int32_t* sources,
                        int k, int threads, uint32_t* dist_out);
 
+/* Grid A* (oracle/search_oracle.cpp): 4-connected width x height grid,
+ * cost[y * width + x] in 1..9 is the cost of entering the cell, 0 an
+ * obstacle; from (0, 0) to (width-1, height-1), Manhattan heuristic.
+ * Returns the optimal path cost or UINT32_MAX when the goal is unreachable;
+ * expansions / max_open (may be NULL) report the search's size. */
+uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* expansions, long long* max_open);
+/* k grids, grid i at costs + offsets[i]; one grid per task on `threads` threads. */
+void gho_astar_grid_many(int k, const int32_t* widths, const int32_t* heights, const int64_t* offsets,
+                         const uint8_t* costs, int threads, uint32_t* out);
+
+/* 0/1 knapsack: best-first branch-and-bound on the Dantzig bound (returns the
+ * optimum; nodes / max_open may be NULL) and the capacity DP cross-check. */
+long long gho_knap_bb(int n, const int32_t* w, const int32_t* p, long long cap, long long* nodes, long long* max_open);
+long long gho_knap_dp(int n, const int32_t* w, const int32_t* p, long long cap);
+/* k instances, instance i: sizes[i] items at w/p + offsets[i], capacity caps[i]. */
+void gho_knap_bb_many(int k, const int32_t* sizes, const int64_t* offsets, const int32_t* w, const int32_t* p,
+                      const int64_t* caps, int threads, int64_t* out);
+
 /* Closed-form algorithmic byte count of one heap-sort (bytes moved by the
  * BGPQ node traffic, independent of the implementation). */
 double gho_sort_bytes(uint64_t n, int batch_size, int key_bytes, int partial_buffer);

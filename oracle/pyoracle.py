@@ -23,7 +23,7 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        src = [os.path.join(HERE, f) for f in ("bgpq_oracle.cpp", "bgpq_oracle.h")]
+        src = [os.path.join(HERE, f) for f in ("bgpq_oracle.cpp", "search_oracle.cpp", "bgpq_oracle.h")]
         if not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in src):
             subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
         so = ctypes.CDLL(LIB)
@@ -43,6 +43,14 @@ def lib():
         so.gho_reversed_idx.argtypes = [ctypes.c_uint32]
         so.gho_dijkstra.argtypes = [ctypes.c_int, _VP, _VP, _VP, ctypes.c_int, _VP]
         so.gho_dijkstra_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int, _VP]
+        so.gho_astar_grid.restype = ctypes.c_uint32
+        so.gho_astar_grid.argtypes = [ctypes.c_int, ctypes.c_int, _VP, _VP, _VP]
+        so.gho_astar_grid_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, ctypes.c_int, _VP]
+        so.gho_knap_bb.restype = ctypes.c_longlong
+        so.gho_knap_bb.argtypes = [ctypes.c_int, _VP, _VP, ctypes.c_longlong, _VP, _VP]
+        so.gho_knap_dp.restype = ctypes.c_longlong
+        so.gho_knap_dp.argtypes = [ctypes.c_int, _VP, _VP, ctypes.c_longlong]
+        so.gho_knap_bb_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, _VP, ctypes.c_int, _VP]
         so.gho_sort_bytes.restype = ctypes.c_double
         so.gho_sort_bytes.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         _lib = so
@@ -99,6 +107,62 @@ def dijkstra(rowptr, col, w, sources, threads=1):
     out = np.empty((src.size, n), np.uint32)
     lib().gho_dijkstra_many(n, rowptr.ctypes.data, col.ctypes.data, w.ctypes.data, src.ctypes.data, src.size,
                             threads, out.ctypes.data)
+    return out
+
+
+def astar_grid(cost, stats=False):
+    """Optimal 4-connected path cost over a (height, width) uint8 cost grid
+    (0 = obstacle) from the top-left to the bottom-right cell; UINT32_MAX when
+    unreachable.  stats=True also returns (expansions, max_open)."""
+    cost = np.ascontiguousarray(cost, np.uint8)
+    h, w = cost.shape
+    e, m = ctypes.c_longlong(), ctypes.c_longlong()
+    r = lib().gho_astar_grid(w, h, cost.ctypes.data, ctypes.byref(e), ctypes.byref(m))
+    return (r, e.value, m.value) if stats else r
+
+
+def astar_grid_many(grids, threads=None):
+    """Optimal costs of a list of (height, width) uint8 grids, one per task."""
+    th = threads or os.cpu_count() or 1
+    widths = np.asarray([g.shape[1] for g in grids], np.int32)
+    heights = np.asarray([g.shape[0] for g in grids], np.int32)
+    offsets = np.zeros(len(grids), np.int64)
+    offsets[1:] = np.cumsum([g.size for g in grids])[:-1]
+    flat = np.ascontiguousarray(np.concatenate([g.ravel() for g in grids])) if grids else np.zeros(1, np.uint8)
+    out = np.zeros(len(grids), np.uint32)
+    lib().gho_astar_grid_many(len(grids), widths.ctypes.data, heights.ctypes.data, offsets.ctypes.data,
+                              flat.ctypes.data, th, out.ctypes.data)
+    return out
+
+
+def knap_bb(w, p, cap, stats=False):
+    """0/1 knapsack optimum by best-first branch-and-bound (Dantzig bound)."""
+    w = np.ascontiguousarray(w, np.int32)
+    p = np.ascontiguousarray(p, np.int32)
+    nodes, mo = ctypes.c_longlong(), ctypes.c_longlong()
+    r = lib().gho_knap_bb(w.size, w.ctypes.data, p.ctypes.data, int(cap), ctypes.byref(nodes), ctypes.byref(mo))
+    return (r, nodes.value, mo.value) if stats else r
+
+
+def knap_dp(w, p, cap):
+    """0/1 knapsack optimum by the capacity dynamic program."""
+    w = np.ascontiguousarray(w, np.int32)
+    p = np.ascontiguousarray(p, np.int32)
+    return lib().gho_knap_dp(w.size, w.ctypes.data, p.ctypes.data, int(cap))
+
+
+def knap_bb_many(instances, threads=None):
+    """Optima of a list of (w, p, cap) instances, one per task."""
+    th = threads or os.cpu_count() or 1
+    sizes = np.asarray([len(w) for w, _, _ in instances], np.int32)
+    offsets = np.zeros(len(instances), np.int64)
+    offsets[1:] = np.cumsum(sizes)[:-1]
+    W = np.ascontiguousarray(np.concatenate([w for w, _, _ in instances]), np.int32)
+    P = np.ascontiguousarray(np.concatenate([p for _, p, _ in instances]), np.int32)
+    caps = np.asarray([c for _, _, c in instances], np.int64)
+    out = np.zeros(len(instances), np.int64)
+    lib().gho_knap_bb_many(len(instances), sizes.ctypes.data, offsets.ctypes.data, W.ctypes.data, P.ctypes.data,
+                           caps.ctypes.data, th, out.ctypes.data)
     return out
 
 

@@ -1,0 +1,106 @@
+"""Batched searches on the GPU (gh_batch_*): every instance's result equals
+the CPU oracle exactly (A* path costs, knapsack optima), in the persistent,
+graph-replayed and plain per-instance forms, run after run."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+from gpuheap_gb300 import batch as gb  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda(ghlib):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    yield
+
+
+def small_mix(seed=5):
+    rng = np.random.default_rng(seed)
+    inst = []
+    # edge cases: single cell, single row / column, walled-off goal, blocked start
+    inst.append(("astar", np.full((1, 1), 3, np.uint8)))
+    inst.append(("astar", gb.gen_grid(37, 1, height=1, obstacle_per_mille=0)))
+    inst.append(("astar", gb.gen_grid(1, 2, height=45, obstacle_per_mille=0)))
+    wall = gb.gen_grid(40, 3, obstacle_per_mille=0)
+    wall[:, 20] = 0
+    inst.append(("astar", wall))
+    blocked = gb.gen_grid(16, 4)
+    blocked[0, 0] = 0
+    inst.append(("astar", blocked))
+    for i in range(20):
+        side = int(rng.integers(8, 300))
+        inst.append(("astar", gb.gen_grid(side, 100 + i, height=int(rng.integers(8, 300)))))
+    # knapsacks: nothing fits, everything fits, one item, random sizes
+    w = np.array([50, 60, 70], np.int32)
+    inst.append(("knapsack", (w, w + 5, 10)))
+    inst.append(("knapsack", (w, w + 5, 1000)))
+    inst.append(("knapsack", (np.array([7], np.int32), np.array([9], np.int32), 7)))
+    for i in range(20):
+        inst.append(("knapsack", gb.gen_knapsack(int(rng.integers(2, 400)), 200 + i)))
+    return inst
+
+
+def oracle_results(inst):
+    grids = [d for k, d in inst if k == "astar"]
+    knaps = [d for k, d in inst if k == "knapsack"]
+    a = iter(pyoracle.astar_grid_many(grids, threads=8))
+    k = iter(pyoracle.knap_bb_many(knaps, threads=8))
+    return np.array([int(next(a)) if kind == "astar" else int(next(k)) for kind, _ in inst], np.int64)
+
+
+@pytest.mark.parametrize("bs,variant", [(64, "bottomup"), (256, "bottomup"), (128, "topdown"), (512, "topdown")])
+def test_batch_matches_oracle_every_mode(bs, variant):
+    inst = small_mix()
+    want = oracle_results(inst)
+    b = gb.Batch(inst, batch_size=bs, variant=variant, astar_cells_per_block=1 << 12)
+    try:
+        for mode in ("persistent", "graph", "graph", "plain", "persistent"):
+            b.run(mode)
+            res, st, stats = b.results()
+            assert not st.any()
+            assert np.array_equal(res, want), (mode, np.nonzero(res != want))
+            assert np.all(stats[:, 0] >= 0)
+    finally:
+        b.close()
+
+
+def test_batch_large_grid_many_blocks():
+    """A 1024^2 grid shared by 8 blocks, next to small instances."""
+    inst = [("astar", gb.gen_grid(1024, 77)), ("astar", gb.gen_grid(300, 78)),
+            ("knapsack", gb.gen_knapsack(1000, 79)), ("knapsack", gb.gen_knapsack(1000, 80))]
+    want = oracle_results(inst)
+    for variant in ("bottomup", "topdown"):
+        b = gb.Batch(inst, batch_size=256, variant=variant, astar_cells_per_block=1 << 17, astar_max_blocks=8)
+        try:
+            assert b.info()["tasks"] == 8 + 1 + 1 + 1
+            for mode in ("graph", "plain"):
+                b.run(mode)
+                res, st, _ = b.results()
+                assert np.array_equal(res, want), (variant, mode)
+        finally:
+            b.close()
+
+
+def test_knapsack_matches_dp():
+    inst = [("knapsack", gb.gen_knapsack(n, 300 + n)) for n in (1, 3, 17, 64, 150)]
+    want = [pyoracle.knap_dp(*d) for _, d in inst]
+    b = gb.Batch(inst, batch_size=64)
+    try:
+        b.run("graph")
+        res, _, _ = b.results()
+        assert list(res) == want
+    finally:
+        b.close()
+
+
+def test_batch_rejects_bad_arguments():
+    with pytest.raises(Exception):
+        gb.Batch([("astar", gb.gen_grid(8, 1))], batch_size=100)
+    with pytest.raises(Exception):
+        gb.Batch([("knapsack", (np.ones(2000, np.int32), np.ones(2000, np.int32), 5))])

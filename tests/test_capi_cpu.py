@@ -52,3 +52,9 @@ def test_rejects_bad_arguments_before_touching_a_device(ghlib):
     assert ghlib.gh_heap_create(None, 0, 0, 1, 16, 128, None) == 1
     assert ghlib.gh_heap_insert(None, None, 0, 0, None) == 1
     assert ghlib.gh_heap_concurrent(None, None, 0, 0, None, 0, None, None) == 1
+    assert ghlib.gh_batch_create(None, 256, 1, 0) == 1
+    assert ghlib.gh_batch_destroy(None) == 1
+    assert ghlib.gh_batch_build(None, None) == 1
+    assert ghlib.gh_batch_run(None, 0, None) == 1
+    assert ghlib.gh_batch_add_astar(None, 4, 4, None, None) == 1
+    assert ghlib.gh_gen_grid(0, 4, 1, 200, None, 1) == 1
