@@ -57,8 +57,12 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--timeout", type=float, default=2.0,
                    help="device wait limit in seconds (raise it under a profiler)")
-    p.add_argument("--workload", choices=["heapsort", "sssp"], default="heapsort",
-                   help="heapsort: the plain heap-sort line (default); sssp: SSSP with the queue")
+    p.add_argument("--workload", choices=["heapsort", "sssp", "batched"], default="heapsort",
+                   help="heapsort: the plain heap-sort line (default); sssp: SSSP with the queue; "
+                        "batched: grid A* + knapsack searches in one persistent launch vs per-instance launches")
+    p.add_argument("--instances", type=int, default=1024, help="batched: searches per step")
+    p.add_argument("--plain-steps", type=int, default=1, help="batched: timed runs of the per-instance launches")
+    p.add_argument("--no-tune", action="store_true", help="batched: skip the autotuner (batch 256, bottom-up)")
     p.add_argument("--scale", type=int, default=22, help="sssp: R-MAT scale")
     p.add_argument("--sources", type=int, default=32, help="sssp: seeded random sources (one per step)")
     p.add_argument("--cpu-sources", type=int, default=16, help="sssp: sources in the CPU Dijkstra sample")
@@ -496,12 +500,117 @@ def sssp_arm(args):
     return 0
 
 
+# ------------------------------------------------------------------ batched searches
+BATCHED_METRIC = "searches/s, {count} grid A* + knapsack instances per launch"
+
+
+def batched_cpu_leg(inst, threads):
+    """The oracle on every instance, one instance per task on `threads` cores."""
+    import numpy as np
+    from oracle import pyoracle
+    t0 = time.perf_counter()
+    grids = [d for k, d in inst if k == "astar"]
+    knaps = [d for k, d in inst if k == "knapsack"]
+    a = iter(pyoracle.astar_grid_many(grids, threads=threads))
+    k = iter(pyoracle.knap_bb_many(knaps, threads=threads))
+    want = np.array([int(next(a)) if kind == "astar" else int(next(k)) for kind, _ in inst], np.int64)
+    return want, time.perf_counter() - t0
+
+
+def batched_arm(args):
+    """One step = every search of the workload once, from scratch, as one
+    graph-replayed persistent launch (fill + seed + search + collect)."""
+    import numpy as np
+    import torch
+
+    import gpuheap_gb300 as gh
+    from gpuheap_gb300 import batch as gb
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    inst = gb.workload(count=args.instances, seed=args.seed)
+    gen_s = time.perf_counter() - t0
+    if args.no_tune:
+        cfg = {"batch_size": 256, "variant": "bottomup", "astar_cells_per_block": 1 << 18, "astar_max_blocks": 8}
+    else:
+        cfg = gb.autotune(inst)
+    b = gb.Batch(inst, batch_size=cfg["batch_size"], variant=cfg["variant"],
+                 astar_cells_per_block=cfg["astar_cells_per_block"], astar_max_blocks=cfg.get("astar_max_blocks", 8),
+                 timeout=args.timeout)
+    info = b.info()
+    stream = torch.cuda.current_stream()
+    for _ in range(max(args.warmup, 1)):
+        b.run("graph", stream)
+    b.results(stream)
+    l0 = gh.launch_count()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            b.run("graph", stream)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+    batched_ms = ev[0].elapsed_time(ev[1]) / args.steps
+    launches = gh.launch_count() - l0
+    res, st, stats = b.results(stream)
+    evp = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    evp[0].record(stream)
+    for _ in range(args.plain_steps):
+        b.run("plain", stream)
+    evp[1].record(stream)
+    torch.cuda.synchronize()
+    plain_ms = evp[0].elapsed_time(evp[1]) / args.plain_steps
+    res_plain, st_plain, _ = b.results(stream)
+    kinds = np.array([0 if k == "astar" else 1 for k, _ in inst])
+    count = len(inst)
+    line = {
+        "metric": BATCHED_METRIC.format(count=count), "value": round(count / (batched_ms / 1e3), 2),
+        "unit": "searches/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(batched_ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"{int((kinds == 0).sum())} grid A* (side log-uniform 256-4096, 20% obstacles, "
+                               f"costs 1-9, Manhattan heuristic) + {int((kinds == 1).sum())} 0/1 knapsack "
+                               f"(100-1000 items, weights 1-1000, profit = weight + U(0,100), capacity half "
+                               f"the weight), seed {args.seed}",
+                   "tuned": cfg, "grid": info["grid"], "tasks": info["tasks"], "block_threads": info["block_threads"],
+                   "arena_bytes": info["arena_bytes"], "generate_s": round(gen_s, 2),
+                   "l2": "grids and distance arrays larger than L2; every step resets them",
+                   "parallelism": f"replicas x{ws}"},
+        "plain_ms_per_step": round(plain_ms, 3),
+        "batched_vs_plain": round(plain_ms / batched_ms, 2),
+        "plain_results_identical": bool(np.array_equal(res, res_plain) and not st_plain.any()),
+        "expansions_per_s": round(float(stats[:, 1].sum()) / (batched_ms / 1e3), 1),
+        "astar_cells": int(sum(d.size for k, d in inst if k == "astar")),
+        "gpu_launches_per_step": round(launches / args.steps, 2),
+        "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        want, cpu_s = batched_cpu_leg(inst, threads)
+        if not np.array_equal(res, want):
+            bad = np.nonzero(res != want)[0]
+            raise SystemExit(f"bench: batched results differ from the CPU oracle at instances {bad[:10].tolist()}")
+        line["exact_vs_cpu"] = f"{count} of {count} instances equal the CPU A* / branch-and-bound optimum"
+        line["cpu_baseline"] = {"value": round(count / cpu_s, 2), "unit": "searches/s", "cores": threads,
+                                "kind": "port", "sample": f"all {count} instances, one per task on {threads} "
+                                                          f"threads (std::priority_queue A*, best-first B&B)"}
+    b.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
     if args.workload == "sssp":
         return sssp_arm(args)
+    if args.workload == "batched":
+        return batched_arm(args)
     return our_arm(args)
 
 

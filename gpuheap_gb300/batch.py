@@ -148,8 +148,9 @@ def _cache_path():
 def autotune(instances, sample=96, seed=7, reps=2, cache=True, log=None):
     """Picks batch size, node layout (bottom-up / top-down) and A* blocks per
     instance for `instances` by timing graph runs of a sample: first batch
-    size x layout at 2^18 cells per block, then the cells per block of the
-    best.  The choice is cached per GPU and workload signature."""
+    size x layout at 2^18 cells per block and at most 8 blocks, then the
+    cells per block, then the block cap, each from the best so far.  The
+    choice is cached per GPU and workload signature."""
     import torch
     sig = {"gpu": torch.cuda.get_device_name(), "count": len(instances),
            "astar_cells": int(sum(d.size for k, d in instances if k == "astar")),
@@ -185,12 +186,17 @@ def autotune(instances, sample=96, seed=7, reps=2, cache=True, log=None):
     best = None
     for bs in (64, 128, 256, 512):
         for v in ("bottomup", "topdown"):
-            cfg = dict(batch_size=bs, variant=v, astar_cells_per_block=1 << 18)
+            cfg = dict(batch_size=bs, variant=v, astar_cells_per_block=1 << 18, astar_max_blocks=8)
             t = trial(cfg)
             if best is None or t < best[1]:
                 best = (cfg, t)
     for c in (1 << 16, 1 << 17, 1 << 19, 1 << 20):
         cfg = dict(best[0], astar_cells_per_block=c)
+        t = trial(cfg)
+        if t < best[1]:
+            best = (cfg, t)
+    for mb in (4, 16, 32):
+        cfg = dict(best[0], astar_max_blocks=mb)
         t = trial(cfg)
         if t < best[1]:
             best = (cfg, t)

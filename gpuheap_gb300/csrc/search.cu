@@ -14,10 +14,13 @@
 //   * knapsack: artifacts/knapsack/models_pq.cuh:52-137 and
 //     knapsackKernel.cuh:4-91 (take a batch of nodes, branch on the item at
 //     the node's level: take it / skip it, prune on the Dantzig bound against
-//     the best profit so far, atomicMax), best-first on the bound: the key is
-//     (INT32_MAX - bound) << 32 | pool slot and the node's (level, profit,
+//     the best profit so far, atomicMax), best-first on the bound with ties
+//     broken deepest first: the key is (INT32_MAX - bound) << 32 |
+//     (1024 - level) << 20 | pool slot, and the node's (level, profit,
 //     weight) sits in the instance's node pool (the reference keeps a 16-byte
-//     record in the heap; here the heap stays on 8-byte keys).
+//     record in the heap; here the heap stays on 8-byte keys).  Taking an
+//     item keeps the parent's bound, so many nodes tie; deepest first reaches
+//     good incumbents early, as a sequential best-first search does.
 //
 // Blocks find work through a task list: an instance appears once per block
 // it should get (large grids several times, knapsacks once), largest first;
@@ -43,6 +46,12 @@ namespace {
 using u64 = unsigned long long;
 constexpr int kMaxKnapItems = 1024;
 constexpr int kMaxSearchThreads = 512;  // 128 registers per thread
+constexpr int kSlotBits = 20;            // knapsack key: pool slot bits below the level
+
+__device__ __forceinline__ u64 knap_key(long long bound, int level, int slot) {
+    return (static_cast<u64>(static_cast<unsigned>(INT_MAX - static_cast<int>(bound))) << 32) |
+           (static_cast<u64>(kMaxKnapItems - level) << kSlotBits) | static_cast<unsigned>(slot);
+}
 
 // One instance, as the kernels see it (device array).
 struct alignas(16) Inst {
@@ -151,7 +160,7 @@ __global__ void k_search_seed(Inst* insts, int count) {
             long long b = in->P[lo];
             if (lo < in->n) b += (in->cap - in->W[lo]) * in->p[lo] / in->w[lo];
             const bool live = b > in->greedy;
-            if (live) in->items[0] = static_cast<u64>(static_cast<unsigned>(INT_MAX - static_cast<int>(b))) << 32;
+            if (live) in->items[0] = knap_key(b, 0, 0);
             st->partialBufferSize = live ? 1 : 0;
         }
     }
@@ -287,9 +296,10 @@ __device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int h
         if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size)) heap.deleteUpdate(heapOff);
         pops += size;
         // read the popped nodes, then return their slots
-        for (int i = tid; i < size; i += T) nodes[i] = pool[static_cast<int>(batch[i] & 0xffffffffu)];
+        constexpr unsigned kSlotMask = (1u << kSlotBits) - 1;
+        for (int i = tid; i < size; i += T) nodes[i] = pool[static_cast<unsigned>(batch[i]) & kSlotMask];
         __syncthreads();
-        for (int i = tid; i < size; i += T) freeList[ctl[3] + i] = static_cast<int>(batch[i] & 0xffffffffu);
+        for (int i = tid; i < size; i += T) freeList[ctl[3] + i] = static_cast<int>(static_cast<unsigned>(batch[i]) & kSlotMask);
         __syncthreads();
         if (tid == 0) ctl[3] += size;
         __syncthreads();
@@ -322,9 +332,7 @@ __device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int h
                         else slot = atomicAdd(&ctl[4], 1);
                         if (slot >= poolCap) { ctl[5] = 1; continue; }
                         pool[slot] = make_int4(level + 1, cp[k], cw[k], 0);
-                        emit[atomicAdd(&ctl[1], 1)] =
-                            (static_cast<u64>(static_cast<unsigned>(INT_MAX - static_cast<int>(cb[k]))) << 32) |
-                            static_cast<unsigned>(slot);
+                        emit[atomicAdd(&ctl[1], 1)] = knap_key(cb[k], level + 1, slot);
                     }
                 }
             }
@@ -635,7 +643,9 @@ gh_status gh_batch_build(gh_batch* b, void* stream) {
             const long long cells = static_cast<long long>(h.width) * h.height;
             blocks[i] = static_cast<int>(std::min<long long>(b->astarMaxBlocks, std::max<long long>(1, cells / b->astarCellsPerBlock)));
         } else {
-            keys = std::max<long long>(1LL << 16, 64LL * B);
+            // batched branch-and-bound explores far more nodes than a
+            // sequential one; pool slots must fit the key's 20 bits
+            keys = std::min<long long>(1LL << 19, std::max<long long>({1LL << 16, 64LL * B, 256LL * static_cast<long long>(h.w.size())}));
         }
         L.bn = heap_nodes(keys, B);
         L.state = off; off = align_up(off + sizeof(gh::HeapState), 256);
@@ -647,7 +657,7 @@ gh_status gh_batch_build(gh_batch* b, void* stream) {
             L.g = off; off = align_up(off + cells * 4, 256);
         } else {
             const int n = static_cast<int>(h.w.size());
-            L.poolCap = (L.bn + 1) * B + 4 * B;
+            L.poolCap = std::min((L.bn + 1) * B + 4 * B, 1 << kSlotBits);
             L.w = off; off = align_up(off + n * 4, 256);
             L.p = off; off = align_up(off + n * 4, 256);
             L.W = off; off = align_up(off + (n + 1) * 8, 256);
