@@ -75,6 +75,17 @@ _SIGS = {
     "gh_batch_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                            ctypes.POINTER(_LL)]),
     "gh_gen_grid": (_I, [_I, _I, ctypes.c_ulonglong, _I, _VP, _I]),
+    "gh_serve_create": (_I, [ctypes.POINTER(_VP), _LL, _I, _I, _I, _I]),
+    "gh_serve_destroy": (_I, [_VP]),
+    "gh_serve_set_blocks": (_I, [_VP, _LL, _I, _LL, _I]),
+    "gh_serve_add_graph": (_I, [_VP, _I, _VP, _VP, _VP, ctypes.POINTER(_I)]),
+    "gh_serve_add_map": (_I, [_VP, _I, _I, _VP, ctypes.POINTER(_I)]),
+    "gh_serve_submit": (_I, [_VP, _I, _I, _I, _I, ctypes.POINTER(_LL)]),
+    "gh_serve_step": (_I, [_VP, _VP, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "gh_serve_result": (_I, [_VP, _LL, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_ulonglong),
+                             ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(_LL)]),
+    "gh_serve_finished": (_I, [_VP, _VP, _I, ctypes.POINTER(_I)]),
+    "gh_serve_info": (_I, [_VP, ctypes.POINTER(_LL), ctypes.POINTER(_LL), ctypes.POINTER(_I), ctypes.POINTER(_LL)]),
 }
 
 _lib = None

@@ -38,370 +38,7 @@
 #include <vector>
 
 #include "gpuheap.h"
-#include "heap_launch.cuh"
-#include "worklist.cuh"
-
-namespace {
-
-using u64 = unsigned long long;
-constexpr int kMaxKnapItems = 1024;
-constexpr int kMaxSearchThreads = 512;  // 128 registers per thread
-constexpr int kSlotBits = 20;            // knapsack key: pool slot bits below the level
-
-__device__ __forceinline__ u64 knap_key(long long bound, int level, int slot) {
-    return (static_cast<u64>(static_cast<unsigned>(INT_MAX - static_cast<int>(bound))) << 32) |
-           (static_cast<u64>(kMaxKnapItems - level) << kSlotBits) | static_cast<unsigned>(slot);
-}
-
-// One instance, as the kernels see it (device array).
-struct alignas(16) Inst {
-    int kind;      // GH_SEARCH_ASTAR / GH_SEARCH_KNAPSACK
-    int blocks;    // blocks that join it
-    int batchNum;  // heap nodes
-    int stop;      // set when an instance-level failure ends the search
-    u64* items;
-    int* status;
-    gh::HeapState* state;
-    // A*
-    int width, height;
-    const unsigned char* cost;
-    unsigned* g;
-    // knapsack: ratio-ordered items and exclusive prefix sums
-    int n, poolCap;
-    long long cap;
-    const int* w;
-    const int* p;
-    const long long* W;
-    const long long* P;
-    int4* pool;  // (level, profit, weight, 0)
-    int* freeList;
-    int freeTop, bump;  // pool allocator, owned by the instance's single block
-    // result and statistics
-    int incumbent;  // A*: best goal cost (as unsigned); knapsack: best profit
-    int failed;     // gh_status of a failure, 0 if none
-    unsigned long long pops, expanded, inserted;
-    int greedy;  // knapsack: profit of the greedy fill (first incumbent)
-};
-
-__device__ __forceinline__ unsigned astar_h(int v, int width, int height) {
-    const int x = v % width, y = v / width;
-    return static_cast<unsigned>((width - 1 - x) + (height - 1 - y));
-}
-
-// Dantzig bound of (level, profit, weight) from shared copies of the prefix
-// sums (restates knapsackKernel.cuh:4-33 with a binary search for the break
-// item and the fractional part floored).
-__device__ __forceinline__ long long knap_bound(const long long* W, const long long* P, const int* w, const int* p,
-                                                int n, long long cap, int level, long long profit, long long weight) {
-    const long long rem = cap - weight;
-    if (rem < 0) return -1;
-    int lo = level, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (W[mid] - W[level] <= rem) lo = mid;
-        else hi = mid - 1;
-    }
-    long long bound = profit + (P[lo] - P[level]);
-    if (lo < n) bound += (rem - (W[lo] - W[level])) * p[lo] / w[lo];
-    return bound;
-}
-
-// Reset of every instance's arrays: heap nodes to init keys, lock words to
-// AVAIL, A* distances to infinity.  blockIdx.y = instance, blockIdx.x = slice.
-__global__ void k_search_fill(Inst* insts, int B) {
-    Inst* in = insts + blockIdx.y;
-    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
-    const size_t first = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const size_t keys = static_cast<size_t>(in->batchNum + 1) * B;
-    for (size_t q = first; q < keys; q += stride) in->items[q] = ~0ull;
-    for (size_t q = first; q < static_cast<size_t>(in->batchNum) + 2; q += stride) in->status[q] = 0;
-    if (in->kind == GH_SEARCH_ASTAR) {
-        const size_t cells = static_cast<size_t>(in->width) * in->height;
-        for (size_t q = first; q < cells; q += stride) in->g[q] = 0xffffffffu;
-    }
-}
-
-// Counters, incumbent and the seed key in the partial buffer (after the fill).
-__global__ void k_search_seed(Inst* insts, int count) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        Inst* in = insts + i;
-        gh::HeapState* st = in->state;
-        st->batchCount = 0;
-        st->deleteCount = 0;
-        st->outLimit = INT_MAX;
-        st->insTicket = 0;
-        st->err = st->errOp = st->errNode = st->errState = 0;
-        st->busy = 0;
-        for (int q = 0; q < 8; ++q) st->appStats[q] = 0;
-        in->stop = 0;
-        in->failed = 0;
-        in->pops = in->expanded = in->inserted = 0;
-        if (in->kind == GH_SEARCH_ASTAR) {
-            const int goal = in->width * in->height - 1;
-            const bool open = in->cost[0] != 0 && in->cost[goal] != 0;
-            in->incumbent = open && goal == 0 ? 0 : static_cast<int>(0xffffffffu);
-            if (open && goal != 0) {
-                in->g[0] = 0;
-                in->items[0] = static_cast<u64>(astar_h(0, in->width, in->height)) << 32;
-            }
-            st->partialBufferSize = open && goal != 0 ? 1 : 0;
-        } else {
-            in->freeTop = 0;
-            in->bump = 1;
-            in->incumbent = in->greedy;
-            in->pool[0] = make_int4(0, 0, 0, 0);
-            // root bound from the global prefix sums (knap_bound with level 0)
-            int lo = 0, hi = in->n;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (in->W[mid] <= in->cap) lo = mid;
-                else hi = mid - 1;
-            }
-            long long b = in->P[lo];
-            if (lo < in->n) b += (in->cap - in->W[lo]) * in->p[lo] / in->w[lo];
-            const bool live = b > in->greedy;
-            if (live) in->items[0] = knap_key(b, 0, 0);
-            st->partialBufferSize = live ? 1 : 0;
-        }
-    }
-}
-
-// Shared memory of a search block, ahead of the heap's region.
-struct SearchSmem {
-    static __host__ __device__ size_t emitKeys(int B, int T) { return static_cast<size_t>(B) + 4 * static_cast<size_t>(T); }
-    static __host__ __device__ size_t bytes(int B, int T) {
-        const size_t keys = (static_cast<size_t>(B) + emitKeys(B, T)) * 8;
-        const size_t knap = static_cast<size_t>(kMaxKnapItems + 1) * 16 + static_cast<size_t>(kMaxKnapItems) * 8 +
-                            static_cast<size_t>(B) * 16;
-        return (keys + knap + 64 + 15) / 16 * 16;
-    }
-};
-
-template <typename H>
-__device__ __forceinline__ void flush_full(const H& heap, u64* emit, int* cnt, int B, int heapOff, unsigned long long& inserted) {
-    __syncthreads();
-    const int c = *cnt;
-    if (c >= B) {
-        heap.insertion(reinterpret_cast<typename H::key_type*>(emit), B, heapOff);
-        for (int i = threadIdx.x; i < c - B; i += blockDim.x) emit[i] = emit[B + i];
-        __syncthreads();
-        if (threadIdx.x == 0) *cnt = c - B;
-        inserted += B;
-    }
-    __syncthreads();
-}
-
-template <typename H>
-__device__ __forceinline__ void flush_rest(const H& heap, u64* emit, int* cnt, int heapOff, unsigned long long& inserted) {
-    __syncthreads();
-    const int c = *cnt;
-    if (c > 0) heap.insertion(reinterpret_cast<typename H::key_type*>(emit), c, heapOff);
-    inserted += c;
-    __syncthreads();
-    if (threadIdx.x == 0) *cnt = 0;
-    __syncthreads();
-}
-
-template <typename H>
-__device__ void run_astar(const H& heap, Inst* in, unsigned char* smem, int heapOff) {
-    const int B = heap.batchSize, T = blockDim.x, tid = threadIdx.x;
-    u64* batch = reinterpret_cast<u64*>(smem);
-    u64* emit = batch + B;
-    int* ctl = reinterpret_cast<int*>(emit + SearchSmem::emitKeys(B, T));
-    const int width = in->width, height = in->height;
-    const int goal = width * height - 1;
-    unsigned* g = in->g;
-    const unsigned char* cost = in->cost;
-    unsigned* inc = reinterpret_cast<unsigned*>(&in->incumbent);
-    unsigned long long pops = 0, expanded = 0, inserted = 0, waitStart = 0;
-    int lastBusy = -1;
-    if (tid == 0) ctl[1] = 0;
-    __syncthreads();
-    for (;;) {
-        if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart)) break;
-        int size = 0;
-        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size)) heap.deleteUpdate(heapOff);
-        pops += size;
-        for (int base = 0; base < size; base += T) {
-            const int i = base + tid;
-            if (i < size) {
-                const u64 key = batch[i];
-                const unsigned f = static_cast<unsigned>(key >> 32);
-                const int v = static_cast<int>(key & 0xffffffffu);
-                const unsigned best = __ldcg(inc);
-                const unsigned hv = astar_h(v, width, height);
-                const unsigned gv = f - hv;
-                if (f < best && gv <= __ldcg(g + v)) {  // not pruned, not stale
-                    ++expanded;
-                    const int x = v % width, y = v / width;
-                    const int nb[4] = {x > 0 ? v - 1 : -1, x + 1 < width ? v + 1 : -1, y > 0 ? v - width : -1,
-                                       y + 1 < height ? v + width : -1};
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int u = nb[k];
-                        if (u < 0) continue;
-                        const unsigned c = cost[u];
-                        if (c == 0) continue;
-                        const unsigned ng = gv + c;
-                        if (u == goal) {
-                            if (ng < __ldcg(g + u)) atomicMin(g + u, ng);
-                            atomicMin(inc, ng);
-                            continue;
-                        }
-                        const unsigned nf = ng + astar_h(u, width, height);
-                        if (nf >= __ldcg(inc) || ng >= __ldcg(g + u)) continue;
-                        if (ng < atomicMin(g + u, ng)) emit[atomicAdd(&ctl[1], 1)] = (static_cast<u64>(nf) << 32) | static_cast<unsigned>(u);
-                    }
-                }
-            }
-            flush_full(heap, emit, &ctl[1], B, heapOff, inserted);
-        }
-        flush_rest(heap, emit, &ctl[1], heapOff, inserted);
-        gh::app::batch_done(heap.state);
-        if (heap.failed()) break;
-    }
-    if (tid == 0) {
-        atomicAdd(&in->pops, pops);
-        atomicAdd(&in->inserted, inserted);
-    }
-    atomicAdd(&in->expanded, expanded);
-}
-
-template <typename H>
-__device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int heapOff) {
-    const int B = heap.batchSize, T = blockDim.x, tid = threadIdx.x;
-    u64* batch = reinterpret_cast<u64*>(smem);
-    u64* emit = batch + B;
-    long long* sW = reinterpret_cast<long long*>(emit + SearchSmem::emitKeys(B, T));
-    long long* sP = sW + kMaxKnapItems + 1;
-    int* sw = reinterpret_cast<int*>(sP + kMaxKnapItems + 1);
-    int* sp = sw + kMaxKnapItems;
-    int4* nodes = reinterpret_cast<int4*>(sp + kMaxKnapItems);
-    int* ctl = reinterpret_cast<int*>(nodes + B);
-    const int n = in->n;
-    const long long cap = in->cap;
-    for (int i = tid; i <= n; i += T) { sW[i] = in->W[i]; sP[i] = in->P[i]; }
-    for (int i = tid; i < n; i += T) { sw[i] = in->w[i]; sp[i] = in->p[i]; }
-    if (tid == 0) { ctl[1] = 0; ctl[3] = in->freeTop; ctl[4] = in->bump; ctl[5] = 0; }
-    __syncthreads();
-    int* best = &in->incumbent;
-    int4* pool = in->pool;
-    int* freeList = in->freeList;
-    const int poolCap = in->poolCap;
-    unsigned long long pops = 0, expanded = 0, inserted = 0, waitStart = 0;
-    int lastBusy = -1;
-    for (;;) {
-        if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart)) break;
-        int size = 0;
-        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size)) heap.deleteUpdate(heapOff);
-        pops += size;
-        // read the popped nodes, then return their slots
-        constexpr unsigned kSlotMask = (1u << kSlotBits) - 1;
-        for (int i = tid; i < size; i += T) nodes[i] = pool[static_cast<unsigned>(batch[i]) & kSlotMask];
-        __syncthreads();
-        for (int i = tid; i < size; i += T) freeList[ctl[3] + i] = static_cast<int>(static_cast<unsigned>(batch[i]) & kSlotMask);
-        __syncthreads();
-        if (tid == 0) ctl[3] += size;
-        __syncthreads();
-        for (int base = 0; base < size; base += T) {
-            const int i = base + tid;
-            if (i < size) {
-                const int4 nd = nodes[i];
-                const int level = nd.x;
-                const long long profit = nd.y, weight = nd.z;
-                const long long b = knap_bound(sW, sP, sw, sp, n, cap, level, profit, weight);
-                if (b > __ldcg(best) && level < n) {
-                    ++expanded;
-                    long long cb[2] = {-1, -1};
-                    int cp[2] = {0, 0}, cw[2] = {0, 0};
-                    if (weight + sw[level] <= cap) {  // take the item
-                        cp[0] = static_cast<int>(profit + sp[level]);
-                        cw[0] = static_cast<int>(weight + sw[level]);
-                        atomicMax(best, cp[0]);
-                        cb[0] = knap_bound(sW, sP, sw, sp, n, cap, level + 1, cp[0], cw[0]);
-                    }
-                    cp[1] = static_cast<int>(profit);  // skip it
-                    cw[1] = static_cast<int>(weight);
-                    cb[1] = knap_bound(sW, sP, sw, sp, n, cap, level + 1, cp[1], cw[1]);
-#pragma unroll
-                    for (int k = 0; k < 2; ++k) {
-                        if (cb[k] <= __ldcg(best)) continue;
-                        int slot;
-                        const int top = atomicSub(&ctl[3], 1) - 1;
-                        if (top >= 0) slot = freeList[top];
-                        else slot = atomicAdd(&ctl[4], 1);
-                        if (slot >= poolCap) { ctl[5] = 1; continue; }
-                        pool[slot] = make_int4(level + 1, cp[k], cw[k], 0);
-                        emit[atomicAdd(&ctl[1], 1)] = knap_key(cb[k], level + 1, slot);
-                    }
-                }
-            }
-            __syncthreads();
-            if (tid == 0 && ctl[3] < 0) ctl[3] = 0;
-            flush_full(heap, emit, &ctl[1], B, heapOff, inserted);
-        }
-        flush_rest(heap, emit, &ctl[1], heapOff, inserted);
-        if (ctl[5]) {  // node pool exhausted
-            if (tid == 0) { in->failed = GH_ERR_CAPACITY; gh::detail::st_relaxed(&in->stop, 1); }
-        }
-        gh::app::batch_done(heap.state);
-        if (heap.failed() || ctl[5]) break;
-    }
-    if (tid == 0) {
-        in->freeTop = ctl[3];
-        in->bump = ctl[4];
-        atomicAdd(&in->pops, pops);
-        atomicAdd(&in->inserted, inserted);
-    }
-    atomicAdd(&in->expanded, expanded);
-}
-
-template <typename H>
-__global__ void __launch_bounds__(kMaxSearchThreads, 1) k_search(H proto, Inst* insts, const int* tasks, int ntasks, int* next) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_task;
-    const int heapOff = static_cast<int>(SearchSmem::bytes(proto.batchSize, blockDim.x) / 4);
-    for (;;) {
-        if (threadIdx.x == 0) s_task = atomicAdd(next, 1);
-        __syncthreads();
-        const int t = s_task;
-        __syncthreads();
-        if (t >= ntasks) break;
-        Inst* in = insts + tasks[t];
-        H h = proto;
-        h.heapItems = reinterpret_cast<typename H::key_type*>(in->items);
-        h.status = in->status;
-        h.state = in->state;
-        h.batchNum = in->batchNum;
-        if (in->kind == GH_SEARCH_ASTAR) run_astar(h, in, smem, heapOff);
-        else run_knapsack(h, in, smem, heapOff);
-        __syncthreads();
-    }
-}
-
-// Records instance failures from the heap's own error word.
-__global__ void k_search_collect(Inst* insts, int count) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        Inst* in = insts + i;
-        const int err = in->state->err;
-        if (err && !in->failed) in->failed = err == gh::kErrCapacity ? GH_ERR_CAPACITY : err == gh::kErrTimeout ? GH_ERR_TIMEOUT : GH_ERR_STATE;
-        if (!in->failed && (in->state->batchCount != 0 || in->state->partialBufferSize != 0) && !in->stop)
-            in->failed = GH_ERR_STATE;
-    }
-}
-
-template <int V, int IPT>
-cudaError_t launch_search(const gh::Heap<uint64_t, V, true, IPT>& proto, Inst* insts, const int* tasks, int ntasks,
-                          int* next, int grid, int threads, size_t smem, cudaStream_t s) {
-    using H = gh::Heap<uint64_t, V, true, IPT>;
-    cudaError_t e = cudaFuncSetAttribute(k_search<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    k_search<H><<<grid, threads, smem, s>>>(proto, insts, tasks, ntasks, next);
-    gh::impl::count_launch();
-    return cudaGetLastError();
-}
-
-}  // namespace
+#include "search_kernels.cuh"
 
 // ---------------------------------------------------------------------- host side
 struct HostInst {
@@ -441,60 +78,13 @@ struct gh_batch {
 
 namespace {
 
-int threads_for(const gh_batch* b) {
-    if (b->threads) return b->threads;
-    return std::min(kMaxSearchThreads, b->batchSize);  // 2 keys per thread per merge (4 at batch 1024)
+SearchConfig config_of(const gh_batch* b) {
+    return SearchConfig{b->batchSize, b->variant, b->threads, b->timeoutNs, b->numSMs};
 }
-
-size_t smem_for(const gh_batch* b) {
-    const int T = threads_for(b);
-    return SearchSmem::bytes(b->batchSize, T) + 16 + gh::Heap<uint64_t, 0, true>::smemBytes(b->batchSize);
-}
-
-int resident_blocks(const gh_batch* b) {
-    int per = 0;
-    const int T = threads_for(b);
-    const size_t smem = smem_for(b);
-    const int ipt = 2 * b->batchSize / T;
-    cudaError_t e = cudaErrorInvalidValue;
-    auto occ = [&](auto kern) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, T, smem);
-    };
-    if (b->variant == GH_TOPDOWN) {
-        if (ipt == 2) e = occ(k_search<gh::Heap<uint64_t, gh::kTopDown, true, 2>>);
-        if (ipt == 4) e = occ(k_search<gh::Heap<uint64_t, gh::kTopDown, true, 4>>);
-    } else {
-        if (ipt == 2) e = occ(k_search<gh::Heap<uint64_t, gh::kBottomUp, true, 2>>);
-        if (ipt == 4) e = occ(k_search<gh::Heap<uint64_t, gh::kBottomUp, true, 4>>);
-    }
-    if (e != cudaSuccess || per < 1) per = 1;
-    return per * b->numSMs;
-}
-
+int threads_for(const gh_batch* b) { return search_threads(config_of(b)); }
+int resident_blocks(const gh_batch* b) { return search_resident_blocks(config_of(b)); }
 cudaError_t launch(const gh_batch* b, const int* tasks, int ntasks, int* next, int grid, cudaStream_t s) {
-    const int T = threads_for(b);
-    const int ipt = 2 * b->batchSize / T;
-    const size_t smem = smem_for(b);
-    auto proto = [&](auto h) {
-        h.heapItems = nullptr;
-        h.status = nullptr;
-        h.state = nullptr;
-        h.init_limits = ~0ull;
-        h.batchNum = 0;
-        h.batchSize = b->batchSize;
-        h.sortOutput = 0;
-        h.timeoutNs = b->timeoutNs;
-        return h;
-    };
-    if (b->variant == GH_TOPDOWN) {
-        if (ipt == 2) return launch_search<gh::kTopDown, 2>(proto(gh::Heap<uint64_t, gh::kTopDown, true, 2>{}), b->insts, tasks, ntasks, next, grid, T, smem, s);
-        if (ipt == 4) return launch_search<gh::kTopDown, 4>(proto(gh::Heap<uint64_t, gh::kTopDown, true, 4>{}), b->insts, tasks, ntasks, next, grid, T, smem, s);
-    } else {
-        if (ipt == 2) return launch_search<gh::kBottomUp, 2>(proto(gh::Heap<uint64_t, gh::kBottomUp, true, 2>{}), b->insts, tasks, ntasks, next, grid, T, smem, s);
-        if (ipt == 4) return launch_search<gh::kBottomUp, 4>(proto(gh::Heap<uint64_t, gh::kBottomUp, true, 4>{}), b->insts, tasks, ntasks, next, grid, T, smem, s);
-    }
-    return cudaErrorInvalidValue;
+    return search_launch(config_of(b), b->insts, tasks, ntasks, next, grid, s, 0);
 }
 
 void free_device(gh_batch* b) {
@@ -710,6 +300,8 @@ gh_status gh_batch_build(gh_batch* b, void* stream) {
         if (h.kind == GH_SEARCH_ASTAR) {
             d.width = h.width;
             d.height = h.height;
+            d.start = 0;
+            d.goal = h.width * h.height - 1;
             d.cost = A + L.cost;
             d.g = reinterpret_cast<unsigned*>(A + L.g);
             if (cudaMemcpyAsync(A + L.cost, h.cost.data(), h.cost.size(), cudaMemcpyHostToDevice, s) != cudaSuccess) return GH_ERR_CUDA;
@@ -816,9 +408,9 @@ namespace {
 gh_status reset_and_run(gh_batch* b, int mode, cudaStream_t s) {
     const int count = static_cast<int>(b->host.size());
     if (cudaMemsetAsync(b->next, 0, static_cast<size_t>(count + 1) * 4, s) != cudaSuccess) return GH_ERR_CUDA;
-    k_search_fill<<<dim3(8, count), 256, 0, s>>>(b->insts, b->batchSize);
+    k_search_fill<<<dim3(8, count), 256, 0, s>>>(b->insts, nullptr, b->batchSize);
     gh::impl::count_launch();
-    k_search_seed<<<(count + 127) / 128, 128, 0, s>>>(b->insts, count);
+    k_search_seed<<<(count + 127) / 128, 128, 0, s>>>(b->insts, nullptr, count);
     gh::impl::count_launch();
     if (cudaGetLastError() != cudaSuccess) return GH_ERR_CUDA;
     if (mode == GH_BATCH_PLAIN) {
@@ -829,7 +421,7 @@ gh_status reset_and_run(gh_batch* b, int mode, cudaStream_t s) {
     } else {
         if (launch(b, b->tasks, b->ntasks, b->next, b->grid, s) != cudaSuccess) return GH_ERR_CUDA;
     }
-    k_search_collect<<<std::max(1, std::min(count / 256 + 1, 1024)), 256, 0, s>>>(b->insts, count);
+    k_search_collect<<<count, 256, 0, s>>>(b->insts, nullptr, 1);
     gh::impl::count_launch();
     return cudaGetLastError() == cudaSuccess ? GH_OK : GH_ERR_CUDA;
 }

@@ -18,6 +18,7 @@
 
 #include "gpuheap.h"
 #include "heap_launch.cuh"
+#include "sssp_relax.cuh"
 #include "worklist.cuh"
 
 struct gh_heap;  // defined in capi.cu; reached through gh_heap_device_view
@@ -109,85 +110,8 @@ __global__ void __launch_bounds__(1024) k_sssp(H heap, const long long* __restri
             continue;
         }
         pops += size;
-        // degrees of the keys that are still current (stale keys expand nothing)
-        for (int i = tid; i < size; i += T) {
-            const u64 key = batch[i];
-            const unsigned d = static_cast<unsigned>(key >> 32);
-            const int v = static_cast<int>(key & 0xffffffffu);
-            pre[i + 1] = d <= __ldcg(dist + v) ? rowptr[v + 1] - rowptr[v] : 0;
-        }
-        __syncthreads();
-        // exclusive scan of the degrees over the block (chunk per thread)
-        const int per = (size + T - 1) / T;
-        long long local = 0;
-        for (int j = 0; j < per; ++j) {
-            const int i = tid * per + j;
-            if (i < size) local += pre[i + 1];
-        }
-        long long incl = local;
-        const int lane = tid & 31, warp = tid >> 5;
-        for (int o = 1; o < 32; o <<= 1) {
-            const long long y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        if (lane == 31) wsum[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            long long x = lane < (T >> 5) ? wsum[lane] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                const long long y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
-            }
-            wsum[lane] = x;
-        }
-        __syncthreads();
-        long long run = incl - local + (warp ? wsum[warp - 1] : 0);
-        for (int j = 0; j < per; ++j) {
-            const int i = tid * per + j;
-            if (i < size) { run += pre[i + 1]; pre[i + 1] = run; }
-        }
-        if (tid == 0) pre[0] = 0;
-        __syncthreads();
-        const long long total = pre[size];
-        edges += total;
-        // relax in rounds of one edge per thread; full batches go to the heap
-        for (long long base = 0; base < total; base += T) {
-            const long long ei = base + tid;
-            if (ei < total) {
-                int lo = 0, hi = size;  // largest lo with pre[lo] <= ei
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (pre[mid] <= ei) lo = mid;
-                    else hi = mid;
-                }
-                const u64 key = batch[lo];
-                const unsigned d = static_cast<unsigned>(key >> 32);
-                const int v = static_cast<int>(key & 0xffffffffu);
-                const long long e = rowptr[v] + (ei - pre[lo]);
-                const int u = col[e];
-                const u64 nd64 = static_cast<u64>(d) + wt[e];
-                const unsigned nd = nd64 >= 0xffffffffULL ? 0xfffffffeu : static_cast<unsigned>(nd64);
-                if (nd < __ldcg(dist + u)) {
-                    const unsigned old = atomicMin(dist + u, nd);
-                    if (nd < old) emit[atomicAdd(&ctl[1], 1)] = (static_cast<u64>(nd) << 32) | static_cast<unsigned>(u);
-                }
-            }
-            __syncthreads();
-            const int cnt = ctl[1];
-            if (cnt >= B) {
-                heap.insertion(reinterpret_cast<typename H::key_type*>(emit), B, heapOff);
-                for (int i = tid; i < cnt - B; i += T) emit[i] = emit[B + i];
-                __syncthreads();
-                if (tid == 0) ctl[1] = cnt - B;
-                inserted += B;
-            }
-            __syncthreads();
-        }
-        const int rest = ctl[1];
-        if (rest > 0) heap.insertion(reinterpret_cast<typename H::key_type*>(emit), rest, heapOff);
-        inserted += rest;
-        __syncthreads();
-        if (tid == 0) ctl[1] = 0;
+        gh::app::sssp_relax_batch(heap, batch, size, pre, wsum, emit, &ctl[1], rowptr, col, wt, dist, heapOff, edges,
+                                  inserted);
         gh::app::batch_done(st);
         if (heap.failed()) break;
     }

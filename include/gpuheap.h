@@ -194,7 +194,7 @@ gh_status gh_sssp(gh_heap* h, int n, const long long* rowptr_dev, const int* col
  * search from scratch.
  * ------------------------------------------------------------------------ */
 typedef struct gh_batch gh_batch;
-typedef enum { GH_SEARCH_ASTAR = 0, GH_SEARCH_KNAPSACK = 1 } gh_search_kind;
+typedef enum { GH_SEARCH_ASTAR = 0, GH_SEARCH_KNAPSACK = 1, GH_SEARCH_SSSP = 2 } gh_search_kind;
 typedef enum { GH_BATCH_PERSISTENT = 0, GH_BATCH_GRAPH = 1, GH_BATCH_PLAIN = 2 } gh_batch_mode;
 
 /* batch_size: power of two in [32, 1024]; block_threads 0 (= min(batch_size,
@@ -234,6 +234,63 @@ gh_status gh_batch_results(gh_batch* b, long long* results, int* status, unsigne
 /* Instances, tasks (block slots), blocks of the persistent launch, block
  * threads and arena bytes (any pointer may be NULL). */
 gh_status gh_batch_info(gh_batch* b, int* count, int* tasks, int* grid, int* threads, long long* arena_bytes);
+
+/* ------------------------------------------------------------------------
+ * Served queries: a continuous-batching loop for SSSP and grid A* queries
+ * of different sizes over resident graphs and maps.  Each admitted query
+ * gets a slot and device memory (its heap and distance array) from one
+ * arena; a query is admitted when a slot and enough memory are free, and
+ * its heap stays on the device between steps.  One step is one persistent
+ * launch over every admitted query in which each block takes at most
+ * `batches_per_step` batches of a query before moving on; queries that
+ * arrive meanwhile are admitted at the next step and their work overlaps on
+ * the device with the others'.  The reference has no serving loop; its
+ * per-query kernels are applications/sssp_longfei_new/sssp.cu:19-132 and
+ * artifacts/astar/pq_model.cuh:299-371.
+ * ------------------------------------------------------------------------ */
+typedef struct gh_server gh_server;
+
+/* arena_bytes of device memory for query state (0 = 60 % of the free
+ * memory), max_slots concurrent queries, batch_size (power of two in
+ * [32, 1024]) / variant of every query's heap (u64 keys, partial buffer),
+ * batches_per_step as above. */
+gh_status gh_serve_create(gh_server** out, long long arena_bytes, int max_slots, int batch_size, int variant,
+                          int batches_per_step);
+gh_status gh_serve_destroy(gh_server* s);
+/* Blocks a query gets in each step: SSSP min(sssp_max_blocks, max(1,
+ * n / vertices_per_block)) (default 2^15 vertices, 64 blocks), A*
+ * min(astar_max_blocks, max(1, cells / cells_per_block)) (default 2^18
+ * cells, 8 blocks).  Applies to queries submitted afterwards. */
+gh_status gh_serve_set_blocks(gh_server* s, long long vertices_per_block, int sssp_max_blocks, long long cells_per_block,
+                              int astar_max_blocks);
+/* Resident datasets; the device arrays stay owned by the caller and must
+ * outlive the server.  CSR graph as in gh_sssp; cost grid as in
+ * gh_batch_add_astar.  *id gets the dataset index. */
+gh_status gh_serve_add_graph(gh_server* s, int n, const long long* rowptr_dev, const int* col_dev,
+                             const unsigned* w_dev, int* id);
+gh_status gh_serve_add_map(gh_server* s, int width, int height, const unsigned char* cost_dev, int* id);
+/* Queues a query: GH_SEARCH_SSSP on graph `dataset` from vertex a (b unused),
+ * or GH_SEARCH_ASTAR on map `dataset` from cell a to cell b.  *query gets its
+ * id.  GH_ERR_CAPACITY if the query could never fit the arena. */
+gh_status gh_serve_submit(gh_server* s, int kind, int dataset, int a, int b, long long* query);
+/* One step: admit queued queries into free slots and memory (in arrival
+ * order, skipping any that do not fit yet), run one launch over every
+ * admitted query, collect the finished ones and free their memory.
+ * Synchronizes the stream.  *finished gets how many queries finished in
+ * this step, *active how many are still admitted, *queued how many wait
+ * (any may be NULL). */
+gh_status gh_serve_step(gh_server* s, void* stream, int* finished, int* active, int* queued);
+/* Results of query `q`: *state 0 queued, 1 admitted, 2 finished, 3 failed;
+ * SSSP: r0 = reachable vertices, r1 = sum of their distances; A*: r0 = the
+ * optimal cost (UINT32_MAX unreachable), r1 = 0; *finish_step = the step in
+ * which it finished.  Any pointer may be NULL. */
+gh_status gh_serve_result(gh_server* s, long long q, int* state, unsigned long long* r0, unsigned long long* r1,
+                          long long* finish_step);
+/* Ids of the queries the last step finished (at most max_ids; *count gets
+ * how many there were). */
+gh_status gh_serve_finished(gh_server* s, long long* ids, int max_ids, int* count);
+/* Arena bytes in use and free, slots in use, steps run (any may be NULL). */
+gh_status gh_serve_info(gh_server* s, long long* used_bytes, long long* free_bytes, int* slots_used, long long* steps);
 
 /* Seeded synthetic cost grid for grid A* (host memory, `threads` host
  * threads): cell i draws r = splitmix64(seed + (i + 1) * golden ratio); it is

@@ -93,6 +93,9 @@ void gho_dijkstra_many(int n, const int64_t* rowptr, const int32_t* col, const u
  * Returns the optimal path cost or UINT32_MAX when the goal is unreachable;
  * expansions / max_open (may be NULL) report the search's size. */
 uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* expansions, long long* max_open);
+/* The same between any start and goal cell (y * width + x). */
+uint32_t gho_astar_grid_sg(int width, int height, const uint8_t* cost, int start, int goal, long long* expansions,
+                           long long* max_open);
 /* k grids, grid i at costs + offsets[i]; one grid per task on `threads` threads. */
 void gho_astar_grid_many(int k, const int32_t* widths, const int32_t* heights, const int64_t* offsets,
                          const uint8_t* costs, int threads, uint32_t* out);

@@ -45,6 +45,8 @@ def lib():
         so.gho_dijkstra_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int, _VP]
         so.gho_astar_grid.restype = ctypes.c_uint32
         so.gho_astar_grid.argtypes = [ctypes.c_int, ctypes.c_int, _VP, _VP, _VP]
+        so.gho_astar_grid_sg.restype = ctypes.c_uint32
+        so.gho_astar_grid_sg.argtypes = [ctypes.c_int, ctypes.c_int, _VP, ctypes.c_int, ctypes.c_int, _VP, _VP]
         so.gho_astar_grid_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, ctypes.c_int, _VP]
         so.gho_knap_bb.restype = ctypes.c_longlong
         so.gho_knap_bb.argtypes = [ctypes.c_int, _VP, _VP, ctypes.c_longlong, _VP, _VP]
@@ -119,6 +121,13 @@ def astar_grid(cost, stats=False):
     e, m = ctypes.c_longlong(), ctypes.c_longlong()
     r = lib().gho_astar_grid(w, h, cost.ctypes.data, ctypes.byref(e), ctypes.byref(m))
     return (r, e.value, m.value) if stats else r
+
+
+def astar_grid_sg(cost, start, goal):
+    """Optimal path cost between cells start and goal (y * width + x)."""
+    cost = np.ascontiguousarray(cost, np.uint8)
+    h, w = cost.shape
+    return lib().gho_astar_grid_sg(w, h, cost.ctypes.data, int(start), int(goal), None, None)
 
 
 def astar_grid_many(grids, threads=None):

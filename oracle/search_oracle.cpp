@@ -75,18 +75,18 @@ int64_t knap_bound(const KnapSorted& k, int level, int64_t profit, int64_t weigh
 
 extern "C" {
 
-uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* expansions, long long* max_open) {
+uint32_t gho_astar_grid_sg(int width, int height, const uint8_t* cost, int start, int goal, long long* expansions,
+                           long long* max_open) {
     const int64_t cells = static_cast<int64_t>(width) * height;
-    const int tx = width - 1, ty = height - 1;
-    const int goal = static_cast<int>(cells - 1);
+    const int tx = goal % width, ty = goal / width;
     std::vector<uint32_t> g(cells, 0xffffffffu);
-    auto h = [&](int v) { return static_cast<uint32_t>((tx - v % width) + (ty - v / width)); };
+    auto h = [&](int v) { return static_cast<uint32_t>(std::abs(tx - v % width) + std::abs(ty - v / width)); };
     std::priority_queue<uint64_t, std::vector<uint64_t>, std::greater<uint64_t>> open;
     long long exp = 0, mo = 0;
     uint32_t result = 0xffffffffu;
-    if (cost[0] != 0 && cost[goal] != 0) {
-        g[0] = 0;
-        open.push(static_cast<uint64_t>(h(0)) << 32);
+    if (cost[start] != 0 && cost[goal] != 0) {
+        g[start] = 0;
+        open.push((static_cast<uint64_t>(h(start)) << 32) | static_cast<uint32_t>(start));
     }
     while (!open.empty()) {
         mo = std::max<long long>(mo, static_cast<long long>(open.size()));
@@ -112,6 +112,11 @@ uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* e
     if (expansions) *expansions = exp;
     if (max_open) *max_open = mo;
     return result;
+}
+
+uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* expansions, long long* max_open) {
+    return gho_astar_grid_sg(width, height, cost, 0, static_cast<int>(static_cast<int64_t>(width) * height - 1),
+                             expansions, max_open);
 }
 
 void gho_astar_grid_many(int k, const int32_t* widths, const int32_t* heights, const int64_t* offsets,

@@ -58,3 +58,7 @@ def test_rejects_bad_arguments_before_touching_a_device(ghlib):
     assert ghlib.gh_batch_run(None, 0, None) == 1
     assert ghlib.gh_batch_add_astar(None, 4, 4, None, None) == 1
     assert ghlib.gh_gen_grid(0, 4, 1, 200, None, 1) == 1
+    assert ghlib.gh_serve_create(None, 0, 4, 256, 1, 8) == 1
+    assert ghlib.gh_serve_destroy(None) == 1
+    assert ghlib.gh_serve_step(None, None, None, None, None) == 1
+    assert ghlib.gh_serve_submit(None, 2, 0, 0, 0, None) == 1

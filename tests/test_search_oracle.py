@@ -6,7 +6,7 @@ import pytest
 from oracle import pyoracle
 
 
-def grid_dijkstra(cost):
+def grid_dijkstra(cost, start=0, goal=None):
     """Independent check: scipy Dijkstra on the grid's move graph."""
     sp = pytest.importorskip("scipy.sparse")
     csgraph = pytest.importorskip("scipy.sparse.csgraph")
@@ -23,7 +23,10 @@ def grid_dijkstra(cost):
         keep = (c > 0) & (cost.ravel()[src] > 0)
         rows.append(src[keep]); cols.append(dst[keep]); vals.append(c[keep].astype(np.float64))
     m = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(h * w, h * w))
-    d = csgraph.dijkstra(m, indices=0)[h * w - 1]
+    goal = h * w - 1 if goal is None else goal
+    if cost.ravel()[start] == 0:
+        return 0xFFFFFFFF
+    d = csgraph.dijkstra(m, indices=start)[goal]
     return 0xFFFFFFFF if not np.isfinite(d) else int(d)
 
 
@@ -36,6 +39,17 @@ def test_astar_oracle_matches_dijkstra(shape, obst, seed):
     cost[0, 0] = max(cost[0, 0], 1)
     cost[-1, -1] = max(cost[-1, -1], 1)
     assert pyoracle.astar_grid(cost) == grid_dijkstra(cost)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_astar_oracle_any_start_and_goal(seed):
+    rng = np.random.default_rng(40 + seed)
+    h, w = int(rng.integers(3, 40)), int(rng.integers(3, 40))
+    cost = rng.integers(1, 10, (h, w)).astype(np.uint8)
+    cost[rng.random((h, w)) < 0.25] = 0
+    for _ in range(5):
+        s, g = (int(x) for x in rng.integers(0, h * w, 2))
+        assert pyoracle.astar_grid_sg(cost, s, g) == (0 if s == g and cost.ravel()[s] else grid_dijkstra(cost, s, g))
 
 
 def test_astar_oracle_unreachable_and_blocked():
