@@ -57,9 +57,14 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--timeout", type=float, default=2.0,
                    help="device wait limit in seconds (raise it under a profiler)")
-    p.add_argument("--workload", choices=["heapsort", "sssp", "batched"], default="heapsort",
+    p.add_argument("--workload", choices=["heapsort", "sssp", "batched", "served"], default="heapsort",
                    help="heapsort: the plain heap-sort line (default); sssp: SSSP with the queue; "
-                        "batched: grid A* + knapsack searches in one persistent launch vs per-instance launches")
+                        "batched: grid A* + knapsack searches in one persistent launch vs per-instance launches; "
+                        "served: Poisson streams of SSSP + A* queries through the continuous-batching server")
+    p.add_argument("--rates", default="100,500,1000,5000", help="served: arrival rates (req/s)")
+    p.add_argument("--queries", type=int, default=200, help="served: queries per rate")
+    p.add_argument("--plain-queries", type=int, default=48, help="served: queries run alone for the baseline")
+    p.add_argument("--batches-per-step", type=int, default=8, help="served: batches a block takes per query per step")
     p.add_argument("--instances", type=int, default=1024, help="batched: searches per step")
     p.add_argument("--plain-steps", type=int, default=1, help="batched: timed runs of the per-instance launches")
     p.add_argument("--no-tune", action="store_true", help="batched: skip the autotuner (batch 256, bottom-up)")
@@ -603,6 +608,151 @@ def batched_arm(args):
     return 0
 
 
+# ------------------------------------------------------------------ served queries
+SERVED_METRIC = "served queries/s at {rate} req/s offered, mixed SSSP (R-MAT 16-22) + grid A* (256^2-4096^2)"
+SSSP_SCALES = (16, 18, 20, 22)
+MAP_SIDES = (256, 512, 1024, 2048, 4096)
+
+
+def served_queries(graphs, maps, count, seed):
+    """Half SSSP, half A*; within each, size class k (0 = smallest) has weight
+    4^-k, so every class brings about the same work."""
+    import numpy as np
+    from gpuheap_gb300 import serve as gs
+    rng = np.random.default_rng(seed)
+    ws = np.array([4.0 ** -k for k in range(len(graphs))]); ws /= ws.sum()
+    wm = np.array([4.0 ** -k for k in range(len(maps))]); wm /= wm.sum()
+    out = []
+    for _ in range(count):
+        if rng.random() < 0.5:
+            gi = int(rng.choice(len(graphs), p=ws))
+            out.append((gs.SSSP, gi, int(rng.integers(graphs[gi].n)), 0))
+        else:
+            mi = int(rng.choice(len(maps), p=wm))
+            cells = maps[mi].numel()
+            out.append((gs.ASTAR, len(graphs) + mi, int(rng.integers(cells)), int(rng.integers(cells))))
+    return out
+
+
+def served_cpu_leg(graphs_host, maps_host, queries, threads):
+    """Oracle results (SSSP digest, A* cost) of `queries` and the CPU time
+    per query: Dijkstra / A* one query per thread."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import pyoracle
+    ng = len(graphs_host)
+
+    def one(q):
+        k, d, a, b = q
+        if k == 2:
+            dist = pyoracle.dijkstra(*graphs_host[d], [a])[0]
+            fin = dist != 0xFFFFFFFF
+            return int(fin.sum()), int(dist[fin].astype(np.uint64).sum())
+        return int(pyoracle.astar_grid_sg(maps_host[d - ng], a, b)), 0
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(one, queries))
+    return res, time.perf_counter() - t0
+
+
+def served_arm(args):
+    """Per offered rate: `queries` seeded queries arrive by a Poisson process
+    and go through the server (admission by free memory, one launch per step
+    over every admitted query); latency = finish - arrival.  The baseline
+    runs a sample of the same mix one query at a time, each alone on the
+    GPU until it finishes."""
+    import numpy as np
+    import torch
+
+    import gpuheap_gb300 as gh
+    from gpuheap_gb300 import batch as gb
+    from gpuheap_gb300 import serve as gs
+    from gpuheap_gb300 import sssp as gsssp
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    graphs = [gsssp.rmat_graph(s, 16, seed=args.seed + s) for s in SSSP_SCALES]
+    maps_host = [gb.gen_grid(side, args.seed + side) for side in MAP_SIDES]
+    maps = [torch.from_numpy(m).cuda() for m in maps_host]
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+
+    def server(**kw):
+        s = gs.Server(**kw)
+        for g in graphs:
+            s.add_graph(g)
+        for m in maps:
+            s.add_map(m)
+        return s
+
+    rates = [float(r) for r in args.rates.split(",")]
+    srv = server(max_slots=256, batch_size=512, batches_per_step=args.batches_per_step)
+    warm = served_queries(graphs, maps, 8, args.seed + 99)
+    gs.run_stream(srv, warm, np.zeros(len(warm)))
+    per_rate, l0 = [], gh.launch_count()
+    with ClockSampler(local) as clk:
+        for i, rate in enumerate(rates):
+            qs = served_queries(graphs, maps, args.queries, args.seed + i)
+            arr = gs.poisson_arrivals(len(qs), rate, args.seed + 1000 + i)
+            lat, res, makespan, steps = gs.run_stream(srv, qs, arr)
+            bad = [r for r in res if r[0] != gs.FINISHED]
+            if bad:
+                raise SystemExit(f"bench: {len(bad)} served queries failed at {rate} req/s")
+            per_rate.append({"offered_per_s": rate, "queries": len(qs), "served_per_s": round(len(qs) / makespan, 2),
+                             "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
+                             "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
+                             "makespan_s": round(makespan, 3), "steps": steps})
+    launches = gh.launch_count() - l0
+    srv.close()
+    # baseline: a sample of the same mix, one query at a time, each with the whole GPU
+    plain_q = served_queries(graphs, maps, args.plain_queries, args.seed + 777)
+    alone = server(max_slots=1, batch_size=512, batches_per_step=1 << 20, sssp_vertices_per_block=1 << 12,
+                   sssp_max_blocks=1024)
+    secs, res_alone = gs.run_plain(alone, plain_q)
+    alone.close()
+    plain_qps = len(plain_q) / float(secs.sum())
+    mix = served_queries(graphs, maps, args.plain_queries, args.seed + 777)
+    srv = server(max_slots=256, batch_size=512, batches_per_step=args.batches_per_step)
+    _, res_mix, _, _ = gs.run_stream(srv, mix, np.zeros(len(mix)))
+    srv.close()
+    same = [(r[1], r[2]) for r in res_alone] == [(r[1], r[2]) for r in res_mix]
+    top = per_rate[-1]
+    line = {
+        "metric": SERVED_METRIC.format(rate=int(top["offered_per_s"])), "value": top["served_per_s"],
+        "unit": "queries/s", "n_gpus": ws, "steps": len(rates), "warmup": 1,
+        "ms_per_step": round(1e3 * top["makespan_s"], 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"{args.queries} queries per rate: half SSSP on R-MAT scales {list(SSSP_SCALES)} "
+                               f"(edge factor 16, weights 1-1000), half A* on {list(MAP_SIDES)}-side grids "
+                               f"(20% obstacles, costs 1-9) between random cells; size class k weighted 4^-k",
+                   "batch_size": 512, "variant": "bottomup", "max_slots": 256,
+                   "batches_per_step": args.batches_per_step, "setup_s": round(setup_s, 2),
+                   "parallelism": f"replicas x{ws}"},
+        "rates": per_rate, "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+        "plain_per_s": round(plain_qps, 2), "served_vs_plain": round(top["served_per_s"] / plain_qps, 2),
+        "alone_equals_mix": f"{len(plain_q)} queries: {'identical' if same else 'DIFFERENT'} results alone and in the mix",
+        "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    if not same:
+        raise SystemExit("bench: served results differ between alone and in the mix")
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sample = plain_q[:threads]
+        want, cpu_s = served_cpu_leg([g.host() for g in graphs], maps_host, sample, threads)
+        got = [(r[1], r[2]) for r in res_alone[:len(sample)]]
+        if got != want:
+            raise SystemExit("bench: served results differ from the CPU oracle")
+        line["exact_vs_cpu"] = f"{len(sample)} sampled queries equal CPU Dijkstra digests / A* costs"
+        line["cpu_baseline"] = {"value": round(len(sample) / cpu_s, 2), "unit": "queries/s", "cores": threads,
+                                "kind": "port", "sample": f"{len(sample)} queries of the mix, one per thread "
+                                                          f"(std::priority_queue Dijkstra / A*)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -611,6 +761,8 @@ def main():
         return sssp_arm(args)
     if args.workload == "batched":
         return batched_arm(args)
+    if args.workload == "served":
+        return served_arm(args)
     return our_arm(args)
 
 
