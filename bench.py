@@ -62,9 +62,10 @@ def parse():
                         "batched: grid A* + knapsack searches in one persistent launch vs per-instance launches; "
                         "served: Poisson streams of SSSP + A* queries through the continuous-batching server")
     p.add_argument("--rates", default="100,500,1000,5000", help="served: arrival rates (req/s)")
-    p.add_argument("--queries", type=int, default=200, help="served: queries per rate")
+    p.add_argument("--queries", type=int, default=600, help="served: queries per rate")
     p.add_argument("--plain-queries", type=int, default=48, help="served: queries run alone for the baseline")
-    p.add_argument("--batches-per-step", type=int, default=8, help="served: batches a block takes per query per step")
+    p.add_argument("--batches-per-step", type=int, default=32, help="served: batches a block takes per query per step")
+    p.add_argument("--served-batch", type=int, default=1024, help="served: batch size of every query's heap")
     p.add_argument("--instances", type=int, default=1024, help="batched: searches per step")
     p.add_argument("--plain-steps", type=int, default=1, help="batched: timed runs of the per-instance launches")
     p.add_argument("--no-tune", action="store_true", help="batched: skip the autotuner (batch 256, bottom-up)")
@@ -73,8 +74,6 @@ def parse():
     p.add_argument("--cpu-sources", type=int, default=16, help="sssp: sources in the CPU Dijkstra sample")
     args = p.parse_args()
     if args.workload == "sssp":
-        if args.batch == 2048:
-            args.batch = 1024  # the SSSP default batch
         if "--steps" not in sys.argv:
             args.steps = args.sources
     return args
@@ -661,7 +660,7 @@ def served_arm(args):
     and go through the server (admission by free memory, one launch per step
     over every admitted query); latency = finish - arrival.  The baseline
     runs a sample of the same mix one query at a time, each alone on the
-    GPU until it finishes."""
+    GPU, in one launch, until it finishes."""
     import numpy as np
     import torch
 
@@ -688,7 +687,7 @@ def served_arm(args):
         return s
 
     rates = [float(r) for r in args.rates.split(",")]
-    srv = server(max_slots=256, batch_size=512, batches_per_step=args.batches_per_step)
+    srv = server(max_slots=256, batch_size=args.served_batch, batches_per_step=args.batches_per_step)
     warm = served_queries(graphs, maps, 8, args.seed + 99)
     gs.run_stream(srv, warm, np.zeros(len(warm)))
     per_rate, l0 = [], gh.launch_count()
@@ -706,15 +705,39 @@ def served_arm(args):
                              "makespan_s": round(makespan, 3), "steps": steps})
     launches = gh.launch_count() - l0
     srv.close()
-    # baseline: a sample of the same mix, one query at a time, each with the whole GPU
+    # baseline: a sample of the same mix, one query at a time, each alone on the
+    # GPU in the configuration that suits it best: SSSP through the standalone
+    # kernel (gh_sssp, batch 2048 on 24 blocks), A* alone in the engine
     plain_q = served_queries(graphs, maps, args.plain_queries, args.seed + 777)
-    alone = server(max_slots=1, batch_size=512, batches_per_step=1 << 20, sssp_vertices_per_block=1 << 12,
-                   sssp_max_blocks=1024)
-    secs, res_alone = gs.run_plain(alone, plain_q)
+    sssp_heaps = {}
+    alone = server(max_slots=1, batch_size=args.served_batch, batches_per_step=1 << 20)
+    secs, res_alone = [], []
+    for k, d, a, b2 in plain_q:
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        if k == gs.SSSP:
+            if d not in sssp_heaps:
+                sssp_heaps[d] = gsssp.make_heap(graphs[d])
+                t1 = time.perf_counter()
+            dist, _ = gsssp.sssp(sssp_heaps[d], graphs[d], a)
+            torch.cuda.synchronize()
+            secs.append(time.perf_counter() - t1)
+            dv = dist.to(torch.int64) & 0xFFFFFFFF  # u32 distances held in int32
+            fin = dv != 0xFFFFFFFF
+            res_alone.append((gs.FINISHED, int(fin.sum().item()), int(dv[fin].sum().item()), 0))
+        else:
+            q = alone.submit(k, d, a, b2)
+            while q not in alone.step()[0]:
+                pass
+            secs.append(time.perf_counter() - t1)
+            res_alone.append(alone.result(q))
     alone.close()
+    for h in sssp_heaps.values():
+        h.close()
+    secs = np.array(secs)
     plain_qps = len(plain_q) / float(secs.sum())
     mix = served_queries(graphs, maps, args.plain_queries, args.seed + 777)
-    srv = server(max_slots=256, batch_size=512, batches_per_step=args.batches_per_step)
+    srv = server(max_slots=256, batch_size=args.served_batch, batches_per_step=args.batches_per_step)
     _, res_mix, _, _ = gs.run_stream(srv, mix, np.zeros(len(mix)))
     srv.close()
     same = [(r[1], r[2]) for r in res_alone] == [(r[1], r[2]) for r in res_mix]
@@ -727,7 +750,7 @@ def served_arm(args):
         "config": {"workload": f"{args.queries} queries per rate: half SSSP on R-MAT scales {list(SSSP_SCALES)} "
                                f"(edge factor 16, weights 1-1000), half A* on {list(MAP_SIDES)}-side grids "
                                f"(20% obstacles, costs 1-9) between random cells; size class k weighted 4^-k",
-                   "batch_size": 512, "variant": "bottomup", "max_slots": 256,
+                   "batch_size": args.served_batch, "variant": "bottomup", "max_slots": 256,
                    "batches_per_step": args.batches_per_step, "setup_s": round(setup_s, 2),
                    "parallelism": f"replicas x{ws}"},
         "rates": per_rate, "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],

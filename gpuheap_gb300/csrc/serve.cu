@@ -63,7 +63,7 @@ struct gh_server {
     SearchConfig cfg{};
     int maxSlots = 0, batchesPerStep = 0, grid = 0;
     long long ssspPerBlock = 1 << 15, astarPerBlock = 1 << 18;
-    int ssspMaxBlocks = 64, astarMaxBlocks = 8;
+    int ssspMaxBlocks = 24, astarMaxBlocks = 8;  // more blocks on one SSSP heap only add re-expansions
     unsigned char* arena = nullptr;
     size_t arenaBytes = 0, used = 0;
     std::map<size_t, size_t> freeBlocks;  // offset -> bytes, coalesced

@@ -22,7 +22,7 @@ QUEUED, ADMITTED, FINISHED, FAILED = 0, 1, 2, 3
 
 class Server:
     def __init__(self, arena_bytes=0, max_slots=256, batch_size=512, variant="bottomup", batches_per_step=8,
-                 sssp_vertices_per_block=1 << 15, sssp_max_blocks=64, astar_cells_per_block=1 << 18,
+                 sssp_vertices_per_block=1 << 15, sssp_max_blocks=24, astar_cells_per_block=1 << 18,
                  astar_max_blocks=8):
         h = _VP()
         _check(lib().gh_serve_create(ctypes.byref(h), int(arena_bytes), max_slots, batch_size, _VARIANTS[variant],

@@ -52,13 +52,26 @@ def rmat_graph(scale, edge_factor=16, seed=1, a=0.57, b=0.19, c=0.19, max_weight
     return Graph(n, rowptr, d2.to(torch.int32).contiguous(), w2.contiguous())
 
 
-def make_heap(graph, batch_size=1024, variant="bottomup", capacity_keys=None):
-    """A u64-key heap (partial buffer on) large enough for SSSP on `graph`."""
+# SSSP runs fastest with large batches on few blocks: every block that takes
+# a batch at the same time takes keys farther from the minimum, so vertices
+# are expanded again later, and all blocks contend on one root.  On GB300,
+# R-MAT scales 18-22: batch 2048 on 24 blocks beat every other point of a
+# sweep over batch {1024, 2048} x blocks {6 .. 152} (scale 22: 109 ms per
+# source on 24 blocks, 341 ms at batch 1024 on 152).
+SSSP_BATCH, SSSP_BLOCKS = 2048, 24
+
+
+def make_heap(graph, batch_size=SSSP_BATCH, variant="bottomup", capacity_keys=None, blocks=SSSP_BLOCKS):
+    """A u64-key heap (partial buffer on) large enough for SSSP on `graph`,
+    running SSSP on `blocks` blocks (0 = one per SM)."""
     keys = capacity_keys or max(4 * graph.n, graph.m // 2, 1 << 16)
     bn = 1
     while bn * batch_size < keys:
         bn <<= 1
-    return Heap(bn, batch_size, key="u64", variant=variant, partial_buffer=True)
+    h = Heap(bn, batch_size, key="u64", variant=variant, partial_buffer=True)
+    if blocks:
+        h.set_grid(blocks)
+    return h
 
 
 def sssp(heap, graph, source, dist=None, stream=None):

@@ -178,7 +178,11 @@ gh_status gh_rmat_edges(int scale, long long m, double a, double b, double c, un
  * CSR graph with n vertices: rowptr_dev (n + 1, int64), col_dev (int32),
  * w_dev (u32).  dist_dev (n, u32) gets the distances, UINT32_MAX where
  * unreachable.  The heap is reset first.  Synchronizes; stats_host (may be
- * NULL) gets {keys taken, edges scanned, keys inserted}. */
+ * NULL) gets {keys taken, edges scanned, keys inserted}.  It runs on the
+ * heap's grid (gh_heap_set_grid): few blocks with large batches are fastest,
+ * because blocks that take batches at the same time take keys farther from
+ * the minimum and expand vertices again, and all of them contend on the root
+ * (on GB300, R-MAT 18-22: batch 2048 on 24 blocks). */
 gh_status gh_sssp(gh_heap* h, int n, const long long* rowptr_dev, const int* col_dev, const unsigned* w_dev,
                   int source, unsigned* dist_dev, void* stream, unsigned long long* stats_host);
 
@@ -258,7 +262,7 @@ gh_status gh_serve_create(gh_server** out, long long arena_bytes, int max_slots,
                           int batches_per_step);
 gh_status gh_serve_destroy(gh_server* s);
 /* Blocks a query gets in each step: SSSP min(sssp_max_blocks, max(1,
- * n / vertices_per_block)) (default 2^15 vertices, 64 blocks), A*
+ * n / vertices_per_block)) (default 2^15 vertices, 24 blocks), A*
  * min(astar_max_blocks, max(1, cells / cells_per_block)) (default 2^18
  * cells, 8 blocks).  Applies to queries submitted afterwards. */
 gh_status gh_serve_set_blocks(gh_server* s, long long vertices_per_block, int sssp_max_blocks, long long cells_per_block,
