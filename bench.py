@@ -57,10 +57,16 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--timeout", type=float, default=2.0,
                    help="device wait limit in seconds (raise it under a profiler)")
-    p.add_argument("--workload", choices=["heapsort", "sssp", "batched", "served"], default="heapsort",
+    p.add_argument("--workload", choices=["heapsort", "sssp", "batched", "served", "fifo"], default="heapsort",
                    help="heapsort: the plain heap-sort line (default); sssp: SSSP with the queue; "
                         "batched: grid A* + knapsack searches in one persistent launch vs per-instance launches; "
-                        "served: Poisson streams of SSSP + A* queries through the continuous-batching server")
+                        "served: Poisson streams of SSSP + A* queries through the continuous-batching server; "
+                        "fifo: push then pop 2^log2n keys through the device FIFO buffer")
+    p.add_argument("--fifo-chunk", type=int, default=0,
+                   help="fifo: keys per insertToBuffer/deleteFromBuffer (0: one reservation per call)")
+    p.add_argument("--fifo-piece", type=int, default=1024,
+                   help="fifo: piece size of the secondary piece-by-piece measurement (0: skip)")
+    p.add_argument("--fifo-threads", type=int, default=512, help="fifo: threads per block")
     p.add_argument("--rates", default="100,500,1000,5000", help="served: arrival rates (req/s)")
     p.add_argument("--queries", type=int, default=600, help="served: queries per rate")
     p.add_argument("--plain-queries", type=int, default=48, help="served: queries run alone for the baseline")
@@ -776,6 +782,141 @@ def served_arm(args):
     return 0
 
 
+# ------------------------------------------------------------------ FIFO buffer
+FIFO_METRIC = "M keys/s push+pop, 2^{log2n} {key} through the device FIFO buffer"
+
+
+def fifo_cpu_leg(log2n, chunk, reps):
+    """The oracle's sequential Buffer<K> model (numpy ring copies), one thread."""
+    import numpy as np
+    from oracle import pyoracle
+    n = 1 << log2n
+    keys = pyoracle.gen("u32", 7, "uniform", n)
+    times = []
+    for _ in range(reps):
+        m = pyoracle.FifoModel(n, np.uint32)
+        t0 = time.perf_counter()
+        m.push(keys, chunk)
+        got = m.pop(n, chunk)
+        times.append(time.perf_counter() - t0)
+    assert np.array_equal(got, keys)
+    return n / statistics.median(times) / 1e6
+
+
+def fifo_arm(args):
+    """One step = push 2^log2n device-resident keys into an empty ring of that
+    capacity over the whole grid (insertKernel, bufferTest.cu:39-47), then pop
+    them all (deleteKernel, bufferTest.cu:49-56); `chunk` keys per call."""
+    import torch
+
+    import gpuheap_gb300 as gh
+    from gpuheap_gb300.fifo import Fifo
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    n = 1 << args.log2n
+    kb = 8 if args.key == "u64" else 4
+    chunk = args.fifo_chunk
+    keys = gh.gen_keys(args.key, args.seed, "uniform", n)
+    out = torch.empty_like(keys)
+    f = Fifo(n, args.key)
+    f.set_timeout(args.timeout)
+    f.set_launch(threads=args.fifo_threads)
+    info = f.info()
+
+    def step(ev=None):
+        if ev:
+            ev[0].record()
+        f.push(keys, chunk=chunk)
+        if ev:
+            ev[1].record()
+        got = f.pop(out, chunk=chunk, sync=ev is None)
+        if ev:
+            ev[2].record()
+        return got
+
+    for _ in range(max(1, args.warmup)):
+        assert step() == n
+    l0 = gh.launch_count()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            step(evs[i])
+            f.count()  # synchronises; the next push then needs no host-side wait
+        torch.cuda.synchronize()
+    launches = gh.launch_count() - l0
+    t_push = [e[0].elapsed_time(e[1]) for e in evs]
+    t_pop = [e[1].elapsed_time(e[2]) for e in evs]
+    total_ms = sum(t_push) + sum(t_pop)
+    value = n * args.steps / (total_ms / 1e3) / 1e6
+    # pieces from different blocks may interleave: the output must be a
+    # permutation of the input (same multiset, compared sorted on the device)
+    if not torch.equal(torch.sort(out).values, torch.sort(keys).values):
+        raise SystemExit("bench: FIFO output is not a permutation of its input")
+
+    peak, peak_kind = peaks()
+    push_ms, pop_ms = statistics.mean(t_push), statistics.mean(t_pop)
+    dom, dom_ms = ("k_fifo_pop", pop_ms) if pop_ms >= push_ms else ("k_fifo_push", push_ms)
+    algo = 2 * kb * n  # push: read the input + write the ring; pop: read the ring + write the output
+    achieved = algo / (dom_ms / 1e3) / 1e9
+    line = {
+        "metric": FIFO_METRIC.format(log2n=args.log2n, key=args.key), "value": round(value, 1), "unit": "M keys/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.key, "data": "synthetic",
+        "config": {"workload": f"device FIFO: push 2^{args.log2n} {args.key} keys then pop them, ring of 2^{args.log2n}, "
+                               + (f"{chunk} keys per call" if chunk else "one reservation per call"), "n_keys": n, "chunk": chunk, "blocks": info["blocks"],
+                   "threads": info["threads"], "l2": "keys and ring larger than L2 (129 MB); no flush needed",
+                   "parallelism": f"replicas x{ws}"},
+        "push_ms": round(push_ms, 3), "pop_ms": round(pop_ms, 3),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": algo},
+        "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    if args.fifo_piece and chunk == 0:
+        # the reference's call shape: one insertToBuffer / deleteFromBuffer per piece
+        f.push(keys, chunk=args.fifo_piece)
+        f.pop(out, chunk=args.fifo_piece)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        f.push(keys, chunk=args.fifo_piece)
+        e[1].record()
+        assert f.pop(out, chunk=args.fifo_piece) == n
+        e[2].record()
+        torch.cuda.synchronize()
+        ms = e[0].elapsed_time(e[2])
+        line["per_piece"] = {"piece": args.fifo_piece, "value": round(n / (ms / 1e3) / 1e6, 1), "unit": "M keys/s",
+                             "push_ms": round(e[0].elapsed_time(e[1]), 3), "pop_ms": round(e[1].elapsed_time(e[2]), 3),
+                             "note": "pieces publish in reservation order; one hand-off per piece bounds the rate"}
+    if not args.no_e2e:
+        pinned_in = keys.cpu().pin_memory()
+        pinned_out = torch.empty_like(pinned_in).pin_memory()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            keys.copy_(pinned_in, non_blocking=True)
+            f.push(keys, chunk=chunk)
+            assert f.pop(out, chunk=chunk) == n
+            pinned_out.copy_(out, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        line["e2e"] = {"value": round(n * args.steps / (ms / 1e3) / 1e6, 1), "unit": "M keys/s",
+                       "h2d_bytes_per_step": n * kb, "d2h_bytes_per_step": n * kb}
+    if rank == 0 and not args.no_cpu:
+        log2s = min(args.log2n, 26)
+        v = fifo_cpu_leg(log2s, chunk or 65536, 3)
+        line["cpu_baseline"] = {"value": round(v, 1), "unit": "M keys/s", "cores": 1, "kind": "port",
+                                "sample": f"the oracle's sequential Buffer model (numpy ring copies), push then pop "
+                                          f"of 2^{log2s} u32 keys in pieces of {chunk or 65536}, 1 thread"}
+    f.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -786,6 +927,8 @@ def main():
         return batched_arm(args)
     if args.workload == "served":
         return served_arm(args)
+    if args.workload == "fifo":
+        return fifo_arm(args)
     return our_arm(args)
 
 

@@ -86,6 +86,22 @@ _SIGS = {
                              ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(_LL)]),
     "gh_serve_finished": (_I, [_VP, _VP, _I, ctypes.POINTER(_I)]),
     "gh_serve_info": (_I, [_VP, ctypes.POINTER(_LL), ctypes.POINTER(_LL), ctypes.POINTER(_I), ctypes.POINTER(_LL)]),
+    "gh_fifo_create": (_I, [ctypes.POINTER(_VP), _I, _LL]),
+    "gh_fifo_destroy": (_I, [_VP]),
+    "gh_fifo_reset": (_I, [_VP, _VP]),
+    "gh_fifo_set_timeout": (_I, [_VP, ctypes.c_double]),
+    "gh_fifo_set_launch": (_I, [_VP, _I, _I]),
+    "gh_fifo_push": (_I, [_VP, _VP, _LL, _I, _VP]),
+    "gh_fifo_pop": (_I, [_VP, _VP, _LL, _I, ctypes.POINTER(_LL), _VP]),
+    "gh_fifo_concurrent": (_I, [_VP, _VP, _LL, _I, _VP, _LL, ctypes.POINTER(_LL), _VP]),
+    "gh_fifo_count": (_I, [_VP, ctypes.POINTER(_LL)]),
+    "gh_fifo_positions": (_I, [_VP] + [ctypes.POINTER(ctypes.c_ulonglong)] * 4),
+    "gh_fifo_snapshot": (_I, [_VP, _VP, _VP]),
+    "gh_fifo_view_bytes": (ctypes.c_size_t, []),
+    "gh_fifo_device_view": (_I, [_VP, _VP, ctypes.c_size_t]),
+    "gh_fifo_inject_reservation": (_I, [_VP, _LL]),
+    "gh_fifo_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_LL), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                          ctypes.POINTER(_I)]),
 }
 
 _lib = None

@@ -212,3 +212,97 @@ class Model:
             lib().gho_model_destroy(self.h)
         except Exception:
             pass
+
+
+class FifoModel:
+    """Sequential restatement of the reference's Buffer<K>
+    (artifacts/buffer/buffer.cuh:6-218) for replaying single-block runs.
+
+    Positions begin <= read <= write <= end count keys since creation; a slot
+    is position % capacity.  insertToBuffer (buffer.cuh:127-170) reserves
+    [end, end + size), needs end + size - begin <= capacity, writes the keys
+    and publishes by moving write to its end.  deleteFromBuffer
+    (buffer.cuh:172-214) claims min(max, write - read) keys at read, copies
+    them out and frees them by moving begin.  With one block every wait
+    succeeds at once, so this model is exact for it.
+    """
+
+    def __init__(self, capacity, dtype=np.uint32):
+        cap = 1
+        while cap < capacity:
+            cap <<= 1
+        self.capacity = cap
+        self.ring = np.zeros(cap, dtype)
+        self.begin = self.read = self.write = self.end = 0
+
+    def insert(self, keys):
+        size = len(keys)
+        if size == 0:
+            return
+        start = self.end
+        if start + size - self.begin > self.capacity:
+            raise OverflowError("ring full: a lone pusher would wait forever")
+        self.end += size
+        idx = (start + np.arange(size)) % self.capacity
+        self.ring[idx] = keys
+        assert self.write == start
+        self.write = start + size
+
+    def delete(self, max_size):
+        n = min(max_size, self.write - self.read)
+        start = self.read
+        self.read += n
+        out = self.ring[(start + np.arange(n)) % self.capacity].copy()
+        assert self.begin == start
+        self.begin = start + n
+        return out
+
+    def push(self, keys, chunk):
+        """insertKernel with one block: pieces of `chunk` keys in order."""
+        for off in range(0, len(keys), chunk):
+            self.insert(keys[off:off + chunk])
+
+    def pop(self, max_keys, chunk):
+        """deleteKernel with one block: takes until max_keys or empty."""
+        parts = []
+        taken = 0
+        while taken < max_keys:
+            got = self.delete(min(chunk, max_keys - taken))
+            if len(got) == 0:
+                break
+            parts.append(got)
+            taken += len(got)
+        return np.concatenate(parts) if parts else self.ring[:0].copy()
+
+    def positions(self):
+        return (self.begin, self.read, self.write, self.end)
+
+
+def fifo_pieces_ok(inp, out, piece_starts):
+    """Checks a multi-block FIFO run: `out` is a permutation of `inp` (distinct
+    keys) in which every piece [piece_starts[i], piece_starts[i+1]) of the
+    input appears whole and in order (a piece is one insertToBuffer call)."""
+    inp = np.asarray(inp)
+    out = np.asarray(out)
+    if len(inp) != len(out) or not np.array_equal(np.sort(inp), np.sort(out)):
+        return False
+    pos = np.empty(len(out), np.int64)
+    order = np.argsort(out, kind="stable")
+    rank_in = np.argsort(np.argsort(inp, kind="stable"), kind="stable")
+    pos[:] = order[rank_in]  # pos[i] = index in out of inp[i]
+    cont = np.ones(len(inp), bool)
+    cont[np.asarray(piece_starts, np.int64)[np.asarray(piece_starts) < len(inp)]] = False
+    return bool(np.all(pos[1:][cont[1:]] == pos[:-1][cont[1:]] + 1))
+
+
+def fifo_piece_starts(n, chunk, split):
+    """Input indices where insertToBuffer calls start for n keys pushed in
+    pieces of `chunk` (split: each piece as its first third and the rest,
+    bufferTest.cu:19-24)."""
+    starts = []
+    for off in range(0, n, chunk):
+        size = min(chunk, n - off)
+        starts.append(off)
+        if split and size // 3 > 0:
+            starts.append(off + size // 3)
+    return np.asarray(starts, np.int64)
