@@ -75,6 +75,8 @@ def parse():
     p.add_argument("--instances", type=int, default=1024, help="batched: searches per step")
     p.add_argument("--plain-steps", type=int, default=1, help="batched: timed runs of the per-instance launches")
     p.add_argument("--no-tune", action="store_true", help="batched: skip the autotuner (batch 256, bottom-up)")
+    p.add_argument("--batched-config", default="",
+                   help="batched: fixed batch_size,variant,astar_cells_per_block,astar_max_blocks instead of tuning")
     p.add_argument("--scale", type=int, default=22, help="sssp: R-MAT scale")
     p.add_argument("--sources", type=int, default=32, help="sssp: seeded random sources (one per step)")
     p.add_argument("--cpu-sources", type=int, default=16, help="sssp: sources in the CPU Dijkstra sample")
@@ -541,7 +543,11 @@ def batched_arm(args):
     t0 = time.perf_counter()
     inst = gb.workload(count=args.instances, seed=args.seed)
     gen_s = time.perf_counter() - t0
-    if args.no_tune:
+    if args.batched_config:
+        bs, var, cells, mb = args.batched_config.split(",")
+        cfg = {"batch_size": int(bs), "variant": var, "astar_cells_per_block": int(cells),
+               "astar_max_blocks": int(mb), "fixed": True}
+    elif args.no_tune:
         cfg = {"batch_size": 256, "variant": "bottomup", "astar_cells_per_block": 1 << 18, "astar_max_blocks": 8}
     else:
         cfg = gb.autotune(inst)
@@ -565,15 +571,17 @@ def batched_arm(args):
     batched_ms = ev[0].elapsed_time(ev[1]) / args.steps
     launches = gh.launch_count() - l0
     res, st, stats = b.results(stream)
-    evp = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-    torch.cuda.synchronize()
-    evp[0].record(stream)
-    for _ in range(args.plain_steps):
-        b.run("plain", stream)
-    evp[1].record(stream)
-    torch.cuda.synchronize()
-    plain_ms = evp[0].elapsed_time(evp[1]) / args.plain_steps
-    res_plain, st_plain, _ = b.results(stream)
+    plain_ms, res_plain, st_plain = None, res, st
+    if args.plain_steps > 0:
+        evp = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        evp[0].record(stream)
+        for _ in range(args.plain_steps):
+            b.run("plain", stream)
+        evp[1].record(stream)
+        torch.cuda.synchronize()
+        plain_ms = evp[0].elapsed_time(evp[1]) / args.plain_steps
+        res_plain, st_plain, _ = b.results(stream)
     kinds = np.array([0 if k == "astar" else 1 for k, _ in inst])
     count = len(inst)
     line = {
@@ -589,10 +597,11 @@ def batched_arm(args):
                    "arena_bytes": info["arena_bytes"], "generate_s": round(gen_s, 2),
                    "l2": "grids and distance arrays larger than L2; every step resets them",
                    "parallelism": f"replicas x{ws}"},
-        "plain_ms_per_step": round(plain_ms, 3),
-        "batched_vs_plain": round(plain_ms / batched_ms, 2),
-        "plain_results_identical": bool(np.array_equal(res, res_plain) and not st_plain.any()),
+        "plain_ms_per_step": round(plain_ms, 3) if plain_ms else None,
+        "batched_vs_plain": round(plain_ms / batched_ms, 2) if plain_ms else None,
+        "plain_results_identical": bool(np.array_equal(res, res_plain) and not st_plain.any()) if plain_ms else None,
         "expansions_per_s": round(float(stats[:, 1].sum()) / (batched_ms / 1e3), 1),
+        "keys_taken_per_step": int(stats[:, 0].sum()), "keys_inserted_per_step": int(stats[:, 2].sum()),
         "astar_cells": int(sum(d.size for k, d in inst if k == "astar")),
         "gpu_launches_per_step": round(launches / args.steps, 2),
         "gpu_launches": launches, "clocks": clk.summary(),

@@ -42,6 +42,7 @@ _SIGS = {
     "gh_heap_set_grid": (_I, [_VP, _I]),
     "gh_heap_insert": (_I, [_VP, _VP, _LL, _I, _VP]),
     "gh_heap_delete": (_I, [_VP, _VP, _LL, ctypes.POINTER(_LL), _VP]),
+    "gh_heap_delete_below": (_I, [_VP, _VP, _LL, _VP, ctypes.POINTER(_LL), _VP]),
     "gh_heap_concurrent": (_I, [_VP, _VP, _LL, _I, _VP, _LL, ctypes.POINTER(_LL), _VP]),
     "gh_heap_sync": (_I, [_VP, _VP]),
     "gh_heap_insert_batch": (_I, [_VP, _VP, _I, _VP]),
@@ -295,6 +296,17 @@ class Heap:
             return None
         got = _LL()
         _check(lib().gh_heap_delete(self._h, _ptr(out), max_keys, ctypes.byref(got), _stream(stream)), "delete")
+        return got.value
+
+    def delete_below(self, out, threshold, max_keys=None, stream=None):
+        """deleteRoot(items, size, app_t_val) until the smallest key is not
+        below `threshold` (artifacts/astar/BGPQ_B/heap.cuh:260-289): whole
+        batches into out[0, n) in ascending order; returns n."""
+        max_keys = out.numel() if max_keys is None else int(max_keys)
+        t = _KEY_CTYPE[self.key](threshold)
+        got = _LL()
+        _check(lib().gh_heap_delete_below(self._h, _ptr(out), max_keys, ctypes.byref(t), ctypes.byref(got),
+                                          _stream(stream)), "delete_below")
         return got.value
 
     def concurrent(self, keys, out, n=None, chunk=0, max_keys=None, stream=None):

@@ -145,14 +145,21 @@ def _cache_path():
     return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune_cache.json")
 
 
-def autotune(instances, sample=96, seed=7, reps=2, cache=True, log=None):
+def autotune(instances, sample=None, seed=7, reps=2, cache=True, log=None, full=True):
     """Picks batch size, node layout (bottom-up / top-down) and A* blocks per
-    instance for `instances` by timing graph runs of a sample: first batch
-    size x layout at 2^18 cells per block and at most 8 blocks, then the
-    cells per block, then the block cap, each from the best so far.  The
-    choice is cached per GPU and workload signature."""
+    instance for `instances`.  On a sample (default: two instances per SM,
+    so the sample keeps the whole GPU busy as the full set does) it times
+    batch size x layout at 2^18 cells per block and at most 8 blocks, then
+    the cells per block and the block cap from the best.  With `full`, the
+    A* block split -- which decides how the largest grids spread over the
+    GPU and so the tail of the whole run -- is then chosen by timing the
+    whole set: cells per block in {2^18, 2^19, 2^20} x cap in {4, 8} for the
+    best layout, and the runner-up layout at the winning split.  The choice
+    is cached per GPU and workload signature."""
     import torch
-    sig = {"gpu": torch.cuda.get_device_name(), "count": len(instances),
+    if sample is None:
+        sample = 2 * torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    sig = {"gpu": torch.cuda.get_device_name(), "count": len(instances), "full": bool(full),
            "astar_cells": int(sum(d.size for k, d in instances if k == "astar")),
            "knap_items": int(sum(len(d[0]) for k, d in instances if k == "knapsack"))}
     key = json.dumps(sig, sort_keys=True)
@@ -170,26 +177,26 @@ def autotune(instances, sample=96, seed=7, reps=2, cache=True, log=None):
     sub = [instances[i] for i in idx]
     timings = []
 
-    def trial(cfg):
-        b = Batch(sub, **cfg)
+    def trial(cfg, insts=sub, n=reps, tag="sample"):
+        b = Batch(insts, **cfg)
         try:
             b.run("graph")
             b.results()
-            t = time_run(b, "graph", reps)
+            t = time_run(b, "graph", n)
         finally:
             b.close()
-        timings.append(dict(cfg, seconds=t))
+        timings.append(dict(cfg, seconds=t, on=tag))
         if log:
-            log(dict(cfg, seconds=round(t, 5)))
+            log(dict(cfg, seconds=round(t, 5), on=tag))
         return t
 
-    best = None
+    layouts = []
     for bs in (64, 128, 256, 512):
         for v in ("bottomup", "topdown"):
             cfg = dict(batch_size=bs, variant=v, astar_cells_per_block=1 << 18, astar_max_blocks=8)
-            t = trial(cfg)
-            if best is None or t < best[1]:
-                best = (cfg, t)
+            layouts.append((trial(cfg), cfg))
+    layouts.sort(key=lambda x: x[0])
+    best = (layouts[0][1], layouts[0][0])
     for c in (1 << 16, 1 << 17, 1 << 19, 1 << 20):
         cfg = dict(best[0], astar_cells_per_block=c)
         t = trial(cfg)
@@ -200,7 +207,24 @@ def autotune(instances, sample=96, seed=7, reps=2, cache=True, log=None):
         t = trial(cfg)
         if t < best[1]:
             best = (cfg, t)
-    choice = dict(best[0], sample=len(sub), sample_seconds=round(best[1], 5))
+    sample_best = best
+    if full and len(sub) < len(instances):
+        fbest = None
+        for c in (1 << 18, 1 << 19, 1 << 20):
+            for mb in (4, 8):
+                cfg = dict(best[0], astar_cells_per_block=c, astar_max_blocks=mb)
+                t = trial(cfg, instances, 1, "full")
+                if fbest is None or t < fbest[1]:
+                    fbest = (cfg, t)
+        second = layouts[1][1]
+        cfg = dict(second, astar_cells_per_block=fbest[0]["astar_cells_per_block"],
+                   astar_max_blocks=fbest[0]["astar_max_blocks"])
+        t = trial(cfg, instances, 1, "full")
+        if t < fbest[1]:
+            fbest = (cfg, t)
+        best = fbest
+    choice = dict(best[0], sample=len(sub), sample_seconds=round(sample_best[1], 5),
+                  full_seconds=round(best[1], 5) if best is not sample_best else None)
     if cache:
         try:
             data = {}

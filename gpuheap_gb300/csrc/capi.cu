@@ -241,7 +241,11 @@ gh_status gh_heap_insert(gh_heap* h, const void* keys_dev, long long n, int chun
     });
 }
 
-gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long long* n_out, void* stream) {
+namespace {
+// Bulk delete into out_dev in ascending order, stopping at max_keys, at an
+// empty heap or (threshold != NULL) at a smallest key not below *threshold.
+gh_status delete_bulk(gh_heap* h, void* out_dev, long long max_keys, const void* threshold, long long* n_out,
+                      void* stream) {
     if (!h || max_keys < 0 || (max_keys > 0 && !out_dev)) return GH_ERR_INVALID;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int lim = static_cast<int>(std::min<long long>(max_keys, INT_MAX));
@@ -252,7 +256,9 @@ gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long lon
         const gh::impl::LaunchArgs a = args_of(h, s);
         gh_status st = with_key(h, [&](auto k) {
             using K = decltype(k);
-            return gh::impl::launch_erase<K>(a, static_cast<K*>(out_dev));
+            K t{};
+            if (threshold) std::memcpy(&t, threshold, sizeof(K));
+            return gh::impl::launch_erase<K>(a, static_cast<K*>(out_dev), threshold ? &t : nullptr);
         });
         if (st != GH_OK) return st;
     }
@@ -267,6 +273,17 @@ gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long lon
         return device_error(h);
     }
     return GH_OK;
+}
+}  // namespace
+
+gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long long* n_out, void* stream) {
+    return delete_bulk(h, out_dev, max_keys, nullptr, n_out, stream);
+}
+
+gh_status gh_heap_delete_below(gh_heap* h, void* out_dev, long long max_keys, const void* threshold,
+                               long long* n_out, void* stream) {
+    if (!threshold) return GH_ERR_INVALID;
+    return delete_bulk(h, out_dev, max_keys, threshold, n_out, stream);
 }
 
 gh_status gh_heap_concurrent(gh_heap* h, const void* keys_dev, long long n, int chunk, void* out_dev,

@@ -46,18 +46,23 @@ __global__ void __launch_bounds__(1024) k_insert(H h, const K* __restrict__ keys
 // One delete: deleteRoot, then deleteUpdate when it returns true, exactly
 // as the reference's kernels call them.  Returns the number of keys written.
 template <typename H, typename K>
-__device__ __forceinline__ int delete_one(const H& h, K* out) {
+__device__ __forceinline__ int delete_one(const H& h, K* out, K threshold) {
     int size = 0;
-    const bool more = h.deleteRoot(out, size);
+    const bool more = h.deleteRoot(out, size, threshold);
     if (more) h.deleteUpdate(0);
     return size;
 }
-
-// deleteKernel: every block deletes until the heap is empty (or the output
-// limit / an error stops it).
 template <typename H, typename K>
-__global__ void __launch_bounds__(1024) k_delete(H h, K* out) {
-    while (delete_one(h, out) != 0) {}
+__device__ __forceinline__ int delete_one(const H& h, K* out) {
+    return delete_one(h, out, h.init_limits);
+}
+
+// deleteKernel: every block deletes until the heap is empty, or its
+// smallest key is not below `threshold` (deleteRoot's app_t_val), or the
+// output limit / an error stops it.
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_delete(H h, K* out, K threshold) {
+    while (delete_one(h, out, threshold) != 0) {}
 }
 
 // concurrentKernel (test/heap_test.cu:13-38): the first half of the grid

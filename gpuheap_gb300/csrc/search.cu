@@ -421,7 +421,7 @@ gh_status reset_and_run(gh_batch* b, int mode, cudaStream_t s) {
     } else {
         if (launch(b, b->tasks, b->ntasks, b->next, b->grid, s) != cudaSuccess) return GH_ERR_CUDA;
     }
-    k_search_collect<<<count, 256, 0, s>>>(b->insts, nullptr, 1);
+    k_search_collect<<<count, 256, 0, s>>>(b->insts, nullptr, 1, b->batchSize);
     gh::impl::count_launch();
     return cudaGetLastError() == cudaSuccess ? GH_OK : GH_ERR_CUDA;
 }

@@ -86,6 +86,32 @@ struct alignas(16) Inst {
     unsigned long long reached, distSum;  // SSSP: reachable vertices, sum of their distances
 };
 
+// Prune thresholds (the app_t_val of deleteRoot, artifacts/astar/BGPQ_B/
+// heap.cuh:260-289): keys at or above them cannot improve the incumbent, so
+// the search leaves them in the heap and ends when only such keys are left.
+// A*: key f<<32 | cell is expanded only while f < incumbent.
+struct AstarThreshold {
+    const unsigned* incumbent;
+    template <typename H>
+    __device__ __forceinline__ u64 operator()(const H&) const {
+        return static_cast<u64>(__ldcg(incumbent)) << 32;
+    }
+};
+// Knapsack: key (INT_MAX - bound)<<32 | ... is expanded only while bound > best.
+struct KnapThreshold {
+    const int* best;
+    template <typename H>
+    __device__ __forceinline__ u64 operator()(const H&) const {
+        return static_cast<u64>(static_cast<unsigned>(INT_MAX - __ldcg(best))) << 32;
+    }
+};
+
+__device__ __forceinline__ u64 prune_threshold(const Inst* in) {
+    if (in->kind == GH_SEARCH_ASTAR) return static_cast<u64>(static_cast<unsigned>(in->incumbent)) << 32;
+    if (in->kind == GH_SEARCH_KNAPSACK) return static_cast<u64>(static_cast<unsigned>(INT_MAX - in->incumbent)) << 32;
+    return ~0ull;  // SSSP relaxes every key
+}
+
 // Manhattan distance to the goal cell (every move costs at least 1).
 __device__ __forceinline__ unsigned astar_h(int v, int width, int goal) {
     const int x = v % width, y = v / width, gx = goal % width, gy = goal / width;
@@ -231,11 +257,12 @@ __device__ void run_astar(const H& heap, Inst* in, unsigned char* smem, int heap
     int lastBusy = -1, batches = 0;
     if (tid == 0) ctl[1] = 0;
     __syncthreads();
+    const AstarThreshold prune{inc};
     for (;;) {
         if (maxBatches && batches++ == maxBatches) break;
-        if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart)) break;
+        if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
         int size = 0;
-        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size)) heap.deleteUpdate(heapOff);
+        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap))) heap.deleteUpdate(heapOff);
         pops += size;
         for (int base = 0; base < size; base += T) {
             const int i = base + tid;
@@ -305,11 +332,12 @@ __device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int h
     const int poolCap = in->poolCap;
     unsigned long long pops = 0, expanded = 0, inserted = 0, waitStart = 0;
     int lastBusy = -1, batches = 0;
+    const KnapThreshold prune{best};
     for (;;) {
         if (maxBatches && batches++ == maxBatches) break;
-        if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart)) break;
+        if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
         int size = 0;
-        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size)) heap.deleteUpdate(heapOff);
+        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap))) heap.deleteUpdate(heapOff);
         pops += size;
         // read the popped nodes, then return their slots
         constexpr unsigned kSlotMask = (1u << kSlotBits) - 1;
@@ -434,11 +462,12 @@ __global__ void __launch_bounds__(kMaxSearchThreads, 1) k_search(H proto, Inst* 
 
 // After a launch, one block per listed instance (ids == NULL: instance
 // blockIdx.x): records failures from the heap's error word, marks the
-// search done when its heap is empty (no block is inside it once the launch
-// has ended), and for a finished SSSP counts the reachable vertices and sums
-// their distances (the query's digest).  final != 0: every search was run to
-// the end, so a non-empty heap is an error.
-__global__ void k_search_collect(Inst* insts, const int* ids, int final) {
+// search done when its heap holds no key below the prune threshold (no
+// block is inside it once the launch has ended), and for a finished SSSP
+// counts the reachable vertices and sums their distances (the query's
+// digest).  final != 0: every search was run to the end, so a heap with a
+// key below the threshold is an error.
+__global__ void k_search_collect(Inst* insts, const int* ids, int final, int batchSize) {
     Inst* in = insts + (ids ? ids[blockIdx.x] : static_cast<int>(blockIdx.x));
     __shared__ int s_done;
     __shared__ unsigned long long s_red[2][32];
@@ -446,9 +475,11 @@ __global__ void k_search_collect(Inst* insts, const int* ids, int final) {
         const int err = in->state->err;
         if (err && !in->failed)
             in->failed = err == gh::kErrCapacity ? GH_ERR_CAPACITY : err == gh::kErrTimeout ? GH_ERR_TIMEOUT : GH_ERR_STATE;
-        const bool empty = in->state->batchCount == 0 && in->state->partialBufferSize == 0;
-        if (final && !in->failed && !empty && !in->stop) in->failed = GH_ERR_STATE;
-        in->done = in->failed || in->stop || empty;
+        const int bc = in->state->batchCount;
+        const bool empty = bc == 0 && in->state->partialBufferSize == 0;
+        const bool finished = empty || in->items[bc > 0 ? batchSize : 0] >= prune_threshold(in);
+        if (final && !in->failed && !finished && !in->stop) in->failed = GH_ERR_STATE;
+        in->done = in->failed || in->stop || finished;
         s_done = in->done && !in->failed && in->kind == GH_SEARCH_SSSP;
     }
     __syncthreads();

@@ -358,7 +358,7 @@ gh_status gh_serve_step(gh_server* s, void* stream, int* finished, int* active, 
         GH_SCUDA(cudaMemcpyAsync(s->ids, s->hostIds, sizeof(int) * act.size(), cudaMemcpyHostToDevice, st));
         GH_SCUDA(cudaMemsetAsync(s->next, 0, sizeof(int), st));
         GH_SCUDA(search_launch(s->cfg, s->insts, s->tasks, nt, s->next, std::min(s->grid, nt), st, s->batchesPerStep));
-        k_search_collect<<<static_cast<unsigned>(act.size()), 256, 0, st>>>(s->insts, s->ids, 0);
+        k_search_collect<<<static_cast<unsigned>(act.size()), 256, 0, st>>>(s->insts, s->ids, 0, s->cfg.batchSize);
         gh::impl::count_launch();
         GH_SCUDA(cudaGetLastError());
         GH_SCUDA(cudaMemcpyAsync(s->hinst.data(), s->insts, sizeof(Inst) * s->maxSlots, cudaMemcpyDeviceToHost, st));

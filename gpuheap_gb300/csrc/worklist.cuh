@@ -16,15 +16,30 @@
 namespace gh {
 namespace app {
 
-// Thread 0 waits until the heap holds keys (then this block is counted busy
-// and the call returns false: take a batch) or the search is over, `stop`
-// (may be NULL) is set, or the heap has an error (returns true).  Every
-// thread calls it; the result is block-uniform.  `word` is a shared int.
-// A wait with no change of busy for longer than the heap's time limit
-// records a timeout and stops.
-template <typename H>
+// No prune threshold: every key is worth taking.
+struct NoThreshold {
+    template <typename H>
+    __device__ __forceinline__ typename H::key_type operator()(const H& heap) const { return heap.init_limits; }
+};
+
+// Thread 0 waits until the heap holds keys below the prune threshold (then
+// this block is counted busy and the call returns false: take a batch) or
+// the search is over, `stop` (may be NULL) is set, or the heap has an error
+// (returns true).  Every thread calls it; the result is block-uniform.
+// `word` is a shared int.  `threshold(heap)` gives the current threshold
+// (deleteRoot(items, size, app_t_val), artifacts/astar/BGPQ_B/heap.cuh:
+// 260-289): keys at or above it are left in the heap, and the search is over
+// once none below it is left and no block is busy.  A block that finds only
+// such keys waits like one that finds the heap empty: it reads busy and
+// never counts itself, so waiting blocks cannot keep each other alive.  The
+// smallest key is read without locks; while blocks are busy it is a hint
+// (a wrong one costs one empty deleteRoot or one early exit of this block,
+// while busy blocks carry on), and the last block to finish reads it with
+// no other block left inside the heap.  A wait with no change of busy for
+// longer than the heap's time limit records a timeout and stops.
+template <typename H, typename Threshold = NoThreshold>
 __device__ __forceinline__ bool wait_for_keys(const H& heap, int* word, const int* stop, int& lastBusy,
-                                              unsigned long long& waitStart) {
+                                              unsigned long long& waitStart, Threshold threshold = {}) {
     HeapState* st = heap.state;
     if (threadIdx.x == 0) {
         int verdict = 0;
@@ -32,11 +47,14 @@ __device__ __forceinline__ bool wait_for_keys(const H& heap, int* word, const in
             if (stop && detail::ld_relaxed(stop) != 0) { verdict = 1; break; }
             const int bc = detail::ld_relaxed(&st->batchCount);
             const int ps = detail::ld_relaxed(&st->partialBufferSize);
-            if (bc || ps) break;
+            if ((bc || ps) && heap.minKeyHint(bc) < threshold(heap)) break;
             const int b = atomicAdd(&st->busy, 0);
             __threadfence();  // the counters below are read after busy
-            if (b == 0 && detail::ld_relaxed(&st->batchCount) == 0 &&
-                detail::ld_relaxed(&st->partialBufferSize) == 0) { verdict = 1; break; }
+            if (b == 0) {
+                const int bc2 = detail::ld_relaxed(&st->batchCount);
+                const int ps2 = detail::ld_relaxed(&st->partialBufferSize);
+                if ((bc2 == 0 && ps2 == 0) || !(heap.minKeyHint(bc2) < threshold(heap))) { verdict = 1; break; }
+            }
             if (detail::ld_relaxed(&st->err) != 0) { verdict = 1; break; }
             const unsigned long long now = detail::globaltimer();
             if (b != lastBusy || waitStart == 0) { lastBusy = b; waitStart = now; }

@@ -69,6 +69,15 @@ gh_status gh_heap_insert(gh_heap* h, const void* keys_dev, long long n, int chun
  * n_out is not NULL the call synchronizes the stream to read the count. */
 gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long long* n_out, void* stream);
 
+/* deleteRoot(items, size, app_t_val) in a loop (artifacts/astar/BGPQ_B/
+ * heap.cuh:260-289): as gh_heap_delete, but a delete takes nothing once
+ * the heap's smallest key (the root's first, or the partial buffer's when
+ * no full node is left) is not below *threshold (one key of the heap's
+ * kind).  Whole batches are taken, so the output holds every key below the
+ * threshold plus the rest of the last batch; the keys left stay in the heap. */
+gh_status gh_heap_delete_below(gh_heap* h, void* out_dev, long long max_keys, const void* threshold,
+                               long long* n_out, void* stream);
+
 /* concurrentKernel (test/heap_test.cu:13-38, test/partial_heap_test.cu:13-38):
  * one launch in which the first half of the grid inserts keys_dev[0, n) in
  * insertion() calls of `chunk` keys (0 = batch_size) while the second half

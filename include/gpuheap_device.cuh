@@ -6,6 +6,7 @@
 // every thread of a block calls
 //     heap.insertion(items, size, smemOffset)   (heap/tditdd/heap.cuh:536)
 //     heap.deleteRoot(items, size)              (heap/tditdd/heap.cuh:267)
+//     heap.deleteRoot(items, size, threshold)   (artifacts/astar/BGPQ_B/heap.cuh:260)
 //     heap.deleteUpdate(smemOffset)             (heap/tditdd/heap.cuh:345)
 // with the reference's meaning: operations are block-collective, a heap node
 // is a sorted batch of batchSize keys, node 0 is the partial buffer, and
@@ -840,7 +841,14 @@ struct Heap {
     // reference it takes no shared-memory offset: its few broadcast words
     // live in a static __shared__ block, so the caller's dynamic shared
     // memory is untouched.
-    __device__ __forceinline__ bool deleteRoot(K* items, int& size) const {
+    __device__ __forceinline__ bool deleteRoot(K* items, int& size) const { return deleteRoot(items, size, init_limits); }
+
+    // deleteRoot(items, size, app_t_val) (artifacts/astar/BGPQ_B/heap.cuh:
+    // 260-289): takes nothing (size 0) when the smallest key -- the root's
+    // first, or the partial buffer's when no full node is left -- is not
+    // below `threshold`: what is left can be pruned.  The key is read under
+    // the locks that the delete takes anyway.
+    __device__ __forceinline__ bool deleteRoot(K* items, int& size, K threshold) const {
         __shared__ OpCtl dr;
         OpCtl* c = &dr;
         size = 0;
@@ -861,14 +869,18 @@ struct Heap {
                 if (want == 0 || (sortOutput && dc + want > lim)) {
                     unlock(0, 0);
                 } else if (bc == 0) {
-                    c->w[0] = 1;
+                    if (__ldcg(node(0)) < threshold) c->w[0] = 1;
+                    else unlock(0, 0);
                 } else {
                     // deleteUpdate will take node bc (a leaf, usually not in
                     // L2): start pulling it in while this block waits for the root
                     if (bc > 1) detail::prefetch_l2(node(bc), nodeBytes());
                     const bool ok1 = lock(1, 0, L, kSiteLockRoot);
                     c->abort = !ok1;
-                    if (ok1) {
+                    if (ok1 && !(__ldcg(node(1)) < threshold)) {
+                        unlock(1, 0);
+                        unlock(0, 0);
+                    } else if (ok1) {
                         c->w[0] = 2;
                         if (sortOutput) detail::st_relaxed(&state->deleteCount, dc + batchSize);
                     }
@@ -892,6 +904,11 @@ struct Heap {
         size = batchSize;
         return true;
     }
+
+    // The smallest key as last published (the root's first, or the partial
+    // buffer's when no full node is left), read without locks: a hint while
+    // other blocks work on the heap, exact when none does.
+    __device__ __forceinline__ K minKeyHint(int batchCount) const { return __ldcg(node(batchCount > 0 ? 1 : 0)); }
 
     // Only the partial buffer holds keys (:297-315): output and reset it,
     // release node 0.

@@ -245,6 +245,54 @@ def test_empty_heap_and_output_limit():
     h.close()
 
 
+def expected_below(sorted_keys, B, t, pb):
+    """Keys deleteRoot(.., app_t_val) takes from a heap of these keys: whole
+    batches (the B smallest each time) while the smallest key is below t,
+    then the partial buffer's remainder when only it is left."""
+    n = len(sorted_keys)
+    q, r = divmod(n, B) if pb else (n // B, 0)
+    taken = 0
+    for k in range(q):
+        if not sorted_keys[k * B] < t:
+            return taken
+        taken += B
+    if r and sorted_keys[q * B] < t:
+        taken += r
+    return taken
+
+
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("pb", [True, False])
+@pytest.mark.parametrize("key,B", [("u32", 256), ("u64", 1024), ("i32", 512)])
+def test_delete_below_threshold(variant, pb, key, B):
+    """deleteRoot with app_t_val: deletes stop at the first batch whose
+    smallest key is not below the threshold; the rest stays in the heap."""
+    rng = np.random.default_rng(B)
+    n = 40 * B + (B // 3 if pb else 0)
+    keys = pyoracle.gen(key, B + len(key), "uniform", n)
+    want = np.sort(keys)
+    for frac in (0.0, 0.25, 0.5, 0.999, 1.0):
+        idx = min(int(frac * n), n - 1)
+        t = int(want[idx]) if frac < 1.0 else int(want[-1]) + 1
+        if frac == 0.0:
+            t = int(want[0])  # nothing is below the smallest key
+        h = gh.Heap(batch_num_for(n, B), B, key=key, variant=variant, partial_buffer=pb)
+        h.set_grid(int(rng.integers(1, 40)))
+        h.insert(to_dev(keys, key), chunk=B // 3 if pb else B)
+        out = empty_dev(n, key)
+        got = h.delete_below(out, t)
+        exp = expected_below(want, B, t, pb)
+        assert got == exp, (frac, got, exp)
+        assert np.array_equal(to_host(out, key)[:got], want[:got])
+        assert h.item_count() == n - got
+        ok, msg = h.check_insert_heap()
+        assert ok, msg
+        rest = empty_dev(n, key)
+        assert h.delete(rest) == n - got
+        assert np.array_equal(to_host(rest, key)[:n - got], want[got:])
+        h.close()
+
+
 def test_capacity_error():
     B = 64
     h = gh.Heap(4, B, key="u32", variant="bottomup", partial_buffer=False)
