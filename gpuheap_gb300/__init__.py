@@ -43,6 +43,7 @@ _SIGS = {
     "gh_heap_insert": (_I, [_VP, _VP, _LL, _I, _VP]),
     "gh_heap_delete": (_I, [_VP, _VP, _LL, ctypes.POINTER(_LL), _VP]),
     "gh_heap_delete_below": (_I, [_VP, _VP, _LL, _VP, ctypes.POINTER(_LL), _VP]),
+    "gh_heap_gc": (_I, [_VP, _VP, ctypes.POINTER(_LL), _VP]),
     "gh_heap_concurrent": (_I, [_VP, _VP, _LL, _I, _VP, _LL, ctypes.POINTER(_LL), _VP]),
     "gh_heap_sync": (_I, [_VP, _VP]),
     "gh_heap_insert_batch": (_I, [_VP, _VP, _I, _VP]),
@@ -308,6 +309,16 @@ class Heap:
         _check(lib().gh_heap_delete_below(self._h, _ptr(out), max_keys, ctypes.byref(t), ctypes.byref(got),
                                           _stream(stream)), "delete_below")
         return got.value
+
+    def gc(self, threshold=None, stream=None):
+        """Garbage collection (invalidFilter, artifacts/astar/gc.cuh:77-180):
+        keeps the keys below `threshold` (None: every real key) and rebuilds
+        the heap from them on the device; returns the number kept."""
+        t = _KEY_CTYPE[self.key](threshold) if threshold is not None else None
+        kept = _LL()
+        _check(lib().gh_heap_gc(self._h, ctypes.byref(t) if t is not None else None, ctypes.byref(kept),
+                                _stream(stream)), "gc")
+        return kept.value
 
     def concurrent(self, keys, out, n=None, chunk=0, max_keys=None, stream=None):
         """concurrentKernel (test/heap_test.cu:13-38): half the grid inserts

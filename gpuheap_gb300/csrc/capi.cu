@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -284,6 +285,62 @@ gh_status gh_heap_delete_below(gh_heap* h, void* out_dev, long long max_keys, co
                                long long* n_out, void* stream) {
     if (!threshold) return GH_ERR_INVALID;
     return delete_bulk(h, out_dev, max_keys, threshold, n_out, stream);
+}
+
+gh_status gh_heap_gc(gh_heap* h, const void* threshold, long long* kept, void* stream) {
+    if (!h) return GH_ERR_INVALID;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the used nodes, after the stream's work (the reference's invalidFilter
+    // reads batchCount the same way, artifacts/astar/gc.cuh:153-154)
+    int cnt[2] = {0, 0};
+    GH_CUDA(cudaMemcpyAsync(cnt, &h->d.state->batchCount, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+    GH_CUDA(cudaStreamSynchronize(s));
+    static_assert(offsetof(gh::HeapState, partialBufferSize) == offsetof(gh::HeapState, batchCount) + sizeof(int),
+                  "batchCount and partialBufferSize are adjacent");
+    gh_status st = device_error(h);
+    if (st != GH_OK) return st;
+    const size_t held = static_cast<size_t>(cnt[0]) * h->d.batchSize + cnt[1];
+    void* buf = nullptr;
+    GH_CUDA(cudaMallocAsync(&buf, 16 + std::max<size_t>(held, 1) * h->d.keyBytes, s));
+    auto* keptDev = static_cast<unsigned long long*>(buf);
+    void* scratch = static_cast<char*>(buf) + 16;
+    st = GH_OK;
+    cudaError_t e = cudaMemsetAsync(keptDev, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) {
+        const int blocks = std::max(1, std::min(h->numSMs * 8, cnt[0] + 1));
+        const gh::impl::LaunchArgs a = args_of(h, s);
+        st = with_key(h, [&](auto k) -> cudaError_t {
+            using K = decltype(k);
+            K t, fill;
+            std::memcpy(&fill, &h->d.initBits, sizeof(K));
+            if (threshold) std::memcpy(&t, threshold, sizeof(K));
+            else t = fill;
+            gh::impl::k_gc_compact<K><<<blocks, 256, 0, s>>>(static_cast<K*>(h->d.items), h->d.status, h->d.state,
+                                                             h->d.batchSize, t, fill, static_cast<K*>(scratch), keptDev);
+            gh::impl::count_launch();
+            gh::impl::k_gc_reset<<<1, 1, 0, s>>>(h->d.state);
+            gh::impl::count_launch();
+            cudaError_t e2 = cudaGetLastError();
+            if (e2 != cudaSuccess) return e2;
+            return gh::impl::launch_insert_counted<K>(a, static_cast<const K*>(scratch), keptDev, h->d.batchSize);
+        });
+    } else {
+        st = cuda_fail(e);
+    }
+    unsigned long long k = 0;
+    if (st == GH_OK && kept) {
+        e = cudaMemcpyAsync(&k, keptDev, sizeof(k), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) st = cuda_fail(e);
+    }
+    cudaError_t ef = cudaFreeAsync(buf, s);
+    if (st != GH_OK) return st;
+    GH_CUDA(ef);
+    if (kept) {
+        GH_CUDA(cudaStreamSynchronize(s));
+        *kept = static_cast<long long>(k);
+        return device_error(h);
+    }
+    return GH_OK;
 }
 
 gh_status gh_heap_concurrent(gh_heap* h, const void* keys_dev, long long n, int chunk, void* out_dev,

@@ -127,6 +127,62 @@ static __global__ void k_set_output(HeapState* st, int deleteCount, int outLimit
 }
 
 // Result of the device-side heap check.
+// Garbage collection (the reference's invalidFilter + garbageCollection +
+// HeapInsert, artifacts/astar/gc.cuh:77-180, artifacts/knapsack/gc.cuh:
+// 30-180), all on the device.  Step 1: every used node (0 = partial buffer
+// with its partialBufferSize keys, 1..batchCount full) keeps its keys below
+// `threshold` -- a prefix, as nodes are sorted -- appended to `scratch` at a
+// range that one atomicAdd per node claims; the node is refilled with
+// `fill` (init_limits) and its lock word cleared.  The reference claims one
+// slot per key with an atomicAdd.
+template <typename K>
+__global__ void __launch_bounds__(256) k_gc_compact(K* items, int* status, const HeapState* st, int B, K threshold,
+                                                    K fill, K* __restrict__ scratch, unsigned long long* kept) {
+    const int bc = st->batchCount, ps = st->partialBufferSize;
+    __shared__ int s_cnt;
+    __shared__ unsigned long long s_off;
+    for (int i = blockIdx.x; i <= bc; i += gridDim.x) {
+        K* nd = items + static_cast<size_t>(i) * B;
+        const int len = i == 0 ? ps : B;
+        if (threadIdx.x == 0) s_cnt = 0;
+        __syncthreads();
+        int c = 0;
+        for (int j = threadIdx.x; j < len; j += blockDim.x) c += nd[j] < threshold ? 1 : 0;
+        if (c) atomicAdd(&s_cnt, c);
+        __syncthreads();
+        const int cnt = s_cnt;
+        if (threadIdx.x == 0) s_off = cnt ? atomicAdd(kept, static_cast<unsigned long long>(cnt)) : 0;
+        __syncthreads();
+        const unsigned long long off = s_off;
+        for (int j = threadIdx.x; j < cnt; j += blockDim.x) scratch[off + j] = nd[j];
+        __syncthreads();
+        for (int j = threadIdx.x; j < B; j += blockDim.x) nd[j] = fill;
+        if (threadIdx.x == 0) status[i] = 0;
+        __syncthreads();
+    }
+}
+
+// Step 2: the heap is empty again (the output cursor is kept).
+static __global__ void k_gc_reset(HeapState* st) {
+    st->batchCount = 0;
+    st->partialBufferSize = 0;
+}
+
+// Step 3: insertKernel over scratch[0, *n) -- the count is read on the
+// device, so the collection needs no round trip to the host.
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_insert_counted(H h, const K* __restrict__ keys, const unsigned long long* n,
+                                                          int chunk) {
+    const long long total = static_cast<long long>(*n);
+    const long long nchunks = (total + chunk - 1) / chunk;
+    for (long long i = blockIdx.x; i < nchunks; i += gridDim.x) {
+        const long long off = i * chunk;
+        const long long rem = total - off;
+        h.insertion(keys + off, rem < chunk ? static_cast<int>(rem) : chunk, 0);
+        if (h.failed()) return;
+    }
+}
+
 struct CheckResult {
     int badNode;  // smallest failing node (INT_MAX when none)
     int code;     // what failed at badNode (see k_check)

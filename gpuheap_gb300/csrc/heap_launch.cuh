@@ -25,6 +25,8 @@ cudaError_t launch_erase(const LaunchArgs& a, K* out, const K* threshold = nullp
 template <typename K>
 cudaError_t launch_erase_one(const LaunchArgs& a, K* out);
 template <typename K>
+cudaError_t launch_insert_counted(const LaunchArgs& a, const K* keys, const unsigned long long* n, int chunk);
+template <typename K>
 cudaError_t launch_concurrent(const LaunchArgs& a, const K* keys, long long n, int chunk, K* out, long long deletes);
 // Bytes of gh::Heap<K, variant, pb> (IPT chosen at run time) for application kernels.
 template <typename K>
@@ -91,6 +93,20 @@ cudaError_t launch_insert(const LaunchArgs& a, const K* keys, long long n, int c
 }
 
 template <typename K>
+cudaError_t launch_insert_counted(const LaunchArgs& a, const K* keys, const unsigned long long* n, int chunk) {
+    return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
+        using H = decltype(proto);
+        const H h = view_of<H>(*a.d, 1);
+        const size_t smem = H::smemBytes(a.d->batchSize);
+        cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_insert_counted<H, K>), smem);
+        if (e != cudaSuccess) return e;
+        k_insert_counted<H, K><<<a.grid, a.threads, smem, a.stream>>>(h, keys, n, chunk);
+        count_launch();
+        return cudaGetLastError();
+    });
+}
+
+template <typename K>
 cudaError_t launch_erase(const LaunchArgs& a, K* out, const K* threshold) {
     return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
         using H = decltype(proto);
@@ -147,6 +163,7 @@ void device_view(const Desc& d, void* out, size_t* bytes) {
 #define GH_INSTANTIATE_KEY(K)                                                                    \
     template cudaError_t launch_insert<K>(const LaunchArgs&, const K*, long long, int);          \
     template cudaError_t launch_erase<K>(const LaunchArgs&, K*, const K*);                       \
+    template cudaError_t launch_insert_counted<K>(const LaunchArgs&, const K*, const unsigned long long*, int); \
     template cudaError_t launch_erase_one<K>(const LaunchArgs&, K*);                             \
     template cudaError_t launch_concurrent<K>(const LaunchArgs&, const K*, long long, int, K*, long long); \
     template void device_view<K>(const Desc&, void*, size_t*);

@@ -78,6 +78,17 @@ gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long lon
 gh_status gh_heap_delete_below(gh_heap* h, void* out_dev, long long max_keys, const void* threshold,
                                long long* n_out, void* stream);
 
+/* Garbage collection (invalidFilter, artifacts/astar/gc.cuh:77-180 and
+ * artifacts/knapsack/gc.cuh:30-180): keeps the keys strictly below
+ * *threshold (NULL = init_limits: every real key; a heap without the
+ * partial buffer also drops its padding keys) and rebuilds the heap from
+ * them by bulk insertion; the output cursor is kept.  The compaction, the
+ * reset and the reinsertion run on the device back to back (one
+ * synchronisation to size the scratch, like the reference's read of
+ * batchCount).  *kept (may be NULL; then the call returns without waiting
+ * for the device) gets the number of keys kept. */
+gh_status gh_heap_gc(gh_heap* h, const void* threshold, long long* kept, void* stream);
+
 /* concurrentKernel (test/heap_test.cu:13-38, test/partial_heap_test.cu:13-38):
  * one launch in which the first half of the grid inserts keys_dev[0, n) in
  * insertion() calls of `chunk` keys (0 = batch_size) while the second half

@@ -293,6 +293,56 @@ def test_delete_below_threshold(variant, pb, key, B):
         h.close()
 
 
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("pb", [True, False])
+@pytest.mark.parametrize("key,B", [("u32", 256), ("u64", 512), ("i32", 1024)])
+def test_gc_keeps_keys_below_threshold(variant, pb, key, B):
+    """Device GC: after inserts and deletes, gc(t) keeps exactly the keys
+    below t; the rebuilt heap passes checkInsertHeap and deletes them in
+    order.  gc() with no threshold keeps every key."""
+    n = 30 * B + (B // 5 if pb else 0)
+    keys = pyoracle.gen(key, 7 * B, "uniform", n)
+    h = gh.Heap(batch_num_for(n, B), B, key=key, variant=variant, partial_buffer=pb)
+    h.set_grid(16)
+    h.insert(to_dev(keys, key), chunk=B // 2 if pb else B)
+    out = empty_dev(n, key)
+    taken = h.delete(out, max_keys=5 * B)                  # a used heap: deletes moved the last nodes up
+    assert taken == 5 * B
+    left = np.sort(keys)[taken:]
+    assert h.gc() == len(left)                            # keep everything
+    ok, msg = h.check_insert_heap()
+    assert ok, msg
+    t = left[len(left) // 3] if key != "i32" else left[2 * len(left) // 3]
+    kept = h.gc(int(t))
+    want = left[left < t]
+    assert kept == len(want)
+    ok, msg = h.check_insert_heap()
+    assert ok, msg
+    pad = 0 if pb else (-kept) % B                          # the rebuild pads a short last insert
+    assert h.item_count() == kept + pad
+    got = h.delete(out)
+    assert got == kept + pad
+    assert np.array_equal(to_host(out, key)[:kept], want)
+    h.close()
+
+
+def test_gc_empty_and_all_dropped():
+    B = 128
+    h = gh.Heap(16, B, key="u32", variant="bottomup")
+    assert h.gc(5) == 0
+    keys = pyoracle.gen("u32", 3, "uniform", 4 * B + 7)
+    h.insert(to_dev(keys, "u32"))
+    assert h.gc(int(keys.min())) == 0                     # nothing is below the smallest key
+    assert h.is_empty()
+    ok, msg = h.check_insert_heap()
+    assert ok, msg
+    h.insert(to_dev(keys, "u32"))                         # the heap works after it
+    out = empty_dev(len(keys), "u32")
+    assert h.delete(out) == len(keys)
+    assert np.array_equal(to_host(out, "u32"), np.sort(keys))
+    h.close()
+
+
 def test_capacity_error():
     B = 64
     h = gh.Heap(4, B, key="u32", variant="bottomup", partial_buffer=False)
