@@ -46,23 +46,30 @@ __global__ void __launch_bounds__(1024) k_insert(H h, const K* __restrict__ keys
 // One delete: deleteRoot, then deleteUpdate when it returns true, exactly
 // as the reference's kernels call them.  Returns the number of keys written.
 template <typename H, typename K>
-__device__ __forceinline__ int delete_one(const H& h, K* out, K threshold) {
+__device__ __forceinline__ int delete_one(const H& h, K* out, K threshold, bool check) {
     int size = 0;
-    const bool more = h.deleteRoot(out, size, threshold);
-    if (more) h.deleteUpdate(0);
+    h.deleteMinImpl(out, size, threshold, check, 0);
+    return size;
+}
+
+// The reference's call pair itself, for the single-operation kernel.
+template <typename H, typename K>
+__device__ __forceinline__ int delete_root_update(const H& h, K* out) {
+    int size = 0;
+    if (h.deleteRoot(out, size)) h.deleteUpdate(0);
     return size;
 }
 template <typename H, typename K>
 __device__ __forceinline__ int delete_one(const H& h, K* out) {
-    return delete_one(h, out, h.init_limits);
+    return delete_one(h, out, h.init_limits, false);
 }
 
-// deleteKernel: every block deletes until the heap is empty, or its
-// smallest key is not below `threshold` (deleteRoot's app_t_val), or the
-// output limit / an error stops it.
+// deleteKernel: every block deletes until the heap is empty, or (check)
+// its smallest key is not below `threshold` (deleteRoot's app_t_val), or
+// the output limit / an error stops it.
 template <typename H, typename K>
-__global__ void __launch_bounds__(1024) k_delete(H h, K* out, K threshold) {
-    while (delete_one(h, out, threshold) != 0) {}
+__global__ void __launch_bounds__(1024) k_delete(H h, K* out, K threshold, int check) {
+    while (delete_one(h, out, threshold, check != 0) != 0) {}
 }
 
 // concurrentKernel (test/heap_test.cu:13-38): the first half of the grid
@@ -92,7 +99,7 @@ __global__ void __launch_bounds__(1024) k_concurrent(H h, const K* __restrict__ 
 // One delete by one block; the size goes to *sizeOut.
 template <typename H, typename K>
 __global__ void __launch_bounds__(1024) k_delete_one(H h, K* out, int* sizeOut) {
-    const int size = delete_one(h, out);
+    const int size = delete_root_update(h, out);
     if (threadIdx.x == 0) *sizeOut = size;
 }
 

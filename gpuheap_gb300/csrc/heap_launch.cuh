@@ -114,7 +114,8 @@ cudaError_t launch_erase(const LaunchArgs& a, K* out, const K* threshold) {
         const size_t smem = H::smemBytes(a.d->batchSize);
         cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_delete<H, K>), smem);
         if (e != cudaSuccess) return e;
-        k_delete<H, K><<<a.grid, a.threads, smem, a.stream>>>(h, out, threshold ? *threshold : h.init_limits);
+        k_delete<H, K><<<a.grid, a.threads, smem, a.stream>>>(h, out, threshold ? *threshold : h.init_limits,
+                                                               threshold ? 1 : 0);
         count_launch();
         return cudaGetLastError();
     });

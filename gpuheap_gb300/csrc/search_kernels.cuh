@@ -262,7 +262,7 @@ __device__ void run_astar(const H& heap, Inst* in, unsigned char* smem, int heap
         if (maxBatches && batches++ == maxBatches) break;
         if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
         int size = 0;
-        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap))) heap.deleteUpdate(heapOff);
+        heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap), heapOff);
         pops += size;
         for (int base = 0; base < size; base += T) {
             const int i = base + tid;
@@ -337,7 +337,7 @@ __device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int h
         if (maxBatches && batches++ == maxBatches) break;
         if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
         int size = 0;
-        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap))) heap.deleteUpdate(heapOff);
+        heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap), heapOff);
         pops += size;
         // read the popped nodes, then return their slots
         constexpr unsigned kSlotMask = (1u << kSlotBits) - 1;
@@ -418,7 +418,7 @@ __device__ void run_sssp(const H& heap, Inst* in, unsigned char* smem, int heapO
         if (maxBatches && batches++ == maxBatches) break;
         if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart)) break;
         int size = 0;
-        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size)) heap.deleteUpdate(heapOff);
+        heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, heapOff);
         pops += size;
         if (size > 0)
             gh::app::sssp_relax_batch(heap, batch, size, pre, wsum, emit, &ctl[1], in->rowptr, in->col, in->wt, in->g,

@@ -4,8 +4,9 @@
 // The caller pattern of applications/sssp_longfei_new/sssp.cu:19-132 (take a
 // batch of (dist << 32 | vertex) keys, drop stale ones, relax the edges of
 // the rest with atomicMin, insert the improved keys), written against this
-// repository's device API (gh::Heap<uint64_t, ...>::deleteRoot /
-// deleteUpdate / insertion) instead of that application's own heap.  Keys
+// repository's device API (gh::Heap<uint64_t, ...>::deleteMin -- deleteRoot
+// + deleteUpdate in one call -- and insertion) instead of that application's
+// own heap.  Keys
 // come out close to key order but not strictly (many blocks work at once), so
 // a vertex can be improved after it was expanded; it is then re-inserted and
 // expanded again (label correcting), and the final distances equal
@@ -103,7 +104,7 @@ __global__ void __launch_bounds__(1024) k_sssp(H heap, const long long* __restri
     for (;;) {
         if (gh::app::wait_for_keys(heap, &ctl[2], nullptr, lastBusy, waitStart)) break;
         int size = 0;
-        if (heap.deleteRoot(reinterpret_cast<typename H::key_type*>(batch), size)) heap.deleteUpdate(heapOff);
+        heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, heapOff);
         if (size == 0) {  // another block took the last keys first
             gh::app::batch_done(st);
             if (heap.failed()) break;

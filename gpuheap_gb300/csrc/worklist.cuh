@@ -11,6 +11,8 @@
 // a count of active blocks in the same way (applications/sssp_longfei_new/
 // sssp.cu:19-132, artifacts/knapsack/models_pq.cuh:52-137 activeCount).
 #pragma once
+#include <type_traits>
+
 #include "gpuheap_device.cuh"
 
 namespace gh {
@@ -41,19 +43,24 @@ template <typename H, typename Threshold = NoThreshold>
 __device__ __forceinline__ bool wait_for_keys(const H& heap, int* word, const int* stop, int& lastBusy,
                                               unsigned long long& waitStart, Threshold threshold = {}) {
     HeapState* st = heap.state;
+    // with no threshold every key is worth taking, padding keys included
+    auto below = [&](int bc) {
+        if constexpr (std::is_same<Threshold, NoThreshold>::value) return true;
+        else return heap.minKeyHint(bc) < threshold(heap);
+    };
     if (threadIdx.x == 0) {
         int verdict = 0;
         for (;;) {
             if (stop && detail::ld_relaxed(stop) != 0) { verdict = 1; break; }
             const int bc = detail::ld_relaxed(&st->batchCount);
             const int ps = detail::ld_relaxed(&st->partialBufferSize);
-            if ((bc || ps) && heap.minKeyHint(bc) < threshold(heap)) break;
+            if ((bc || ps) && below(bc)) break;
             const int b = atomicAdd(&st->busy, 0);
             __threadfence();  // the counters below are read after busy
             if (b == 0) {
                 const int bc2 = detail::ld_relaxed(&st->batchCount);
                 const int ps2 = detail::ld_relaxed(&st->partialBufferSize);
-                if ((bc2 == 0 && ps2 == 0) || !(heap.minKeyHint(bc2) < threshold(heap))) { verdict = 1; break; }
+                if ((bc2 == 0 && ps2 == 0) || !below(bc2)) { verdict = 1; break; }
             }
             if (detail::ld_relaxed(&st->err) != 0) { verdict = 1; break; }
             const unsigned long long now = detail::globaltimer();

@@ -841,7 +841,9 @@ struct Heap {
     // reference it takes no shared-memory offset: its few broadcast words
     // live in a static __shared__ block, so the caller's dynamic shared
     // memory is untouched.
-    __device__ __forceinline__ bool deleteRoot(K* items, int& size) const { return deleteRoot(items, size, init_limits); }
+    __device__ __forceinline__ bool deleteRoot(K* items, int& size) const {
+        return deleteRootImpl(items, size, init_limits, false);
+    }
 
     // deleteRoot(items, size, app_t_val) (artifacts/astar/BGPQ_B/heap.cuh:
     // 260-289): takes nothing (size 0) when the smallest key -- the root's
@@ -849,6 +851,12 @@ struct Heap {
     // below `threshold`: what is left can be pruned.  The key is read under
     // the locks that the delete takes anyway.
     __device__ __forceinline__ bool deleteRoot(K* items, int& size, K threshold) const {
+        return deleteRootImpl(items, size, threshold, true);
+    }
+
+    // `check` false: no threshold at all (heap/tditdd/heap.cuh:267), so a heap
+    // without the partial buffer also gives up its padding batches.
+    __device__ __forceinline__ bool deleteRootImpl(K* items, int& size, K threshold, bool check) const {
         __shared__ OpCtl dr;
         OpCtl* c = &dr;
         size = 0;
@@ -869,7 +877,7 @@ struct Heap {
                 if (want == 0 || (sortOutput && dc + want > lim)) {
                     unlock(0, 0);
                 } else if (bc == 0) {
-                    if (__ldcg(node(0)) < threshold) c->w[0] = 1;
+                    if (!check || __ldcg(node(0)) < threshold) c->w[0] = 1;
                     else unlock(0, 0);
                 } else {
                     // deleteUpdate will take node bc (a leaf, usually not in
@@ -877,7 +885,7 @@ struct Heap {
                     if (bc > 1) detail::prefetch_l2(node(bc), nodeBytes());
                     const bool ok1 = lock(1, 0, L, kSiteLockRoot);
                     c->abort = !ok1;
-                    if (ok1 && !(__ldcg(node(1)) < threshold)) {
+                    if (ok1 && check && !(__ldcg(node(1)) < threshold)) {
                         unlock(1, 0);
                         unlock(0, 0);
                     } else if (ok1) {
@@ -945,6 +953,136 @@ struct Heap {
         refill_and_sift(op, base, last);
     }
 
+    // ------------------------------------------------------------------ deleteMin
+    // deleteRoot(items, size, threshold) followed by deleteUpdate(smemOffset)
+    // when it returns true, with the same result, for kernels that hold the
+    // shared-memory region anyway.  Bottom-up: once the root is held, thread 0
+    // takes the last node and one bulk transaction brings root, last node and
+    // partial buffer into shared memory; the root goes to the output from
+    // there.  The split calls read the root from global memory first and only
+    // then take and load the last node, so this shortens the time the root
+    // is held -- the period of back-to-back deletes -- by about one global
+    // round trip.  Top-down keeps the split calls: its last node may be an
+    // insert target whose batch is handed over at the root.
+    __device__ __forceinline__ void deleteMin(K* items, int& size, K threshold, int smemOffset) const {
+        deleteMinImpl(items, size, threshold, true, smemOffset);
+    }
+    __device__ __forceinline__ void deleteMin(K* items, int& size, int smemOffset) const {
+        deleteMinImpl(items, size, init_limits, false, smemOffset);
+    }
+    __device__ __forceinline__ void deleteMinImpl(K* items, int& size, K threshold, bool check, int smemOffset) const {
+        if constexpr (VARIANT == kTopDown) {
+            if (deleteRootImpl(items, size, threshold, check)) deleteUpdate(smemOffset);
+        } else {
+            deleteMinBottomUp(items, size, threshold, check, smemOffset);
+        }
+    }
+
+    __device__ __forceinline__ void deleteMinBottomUp(K* items, int& size, K threshold, bool check,
+                                                      int smemOffset) const {
+        K* base = region(smemOffset);
+        Op op(this, ctl(base));
+        OpCtl* c = op.c;
+        const int B = batchSize;
+        const int tid = threadIdx.x;
+        K* C = base;
+        K* P = base + B;
+        K* R = base + 2 * B;  // the root; the sift's first child buffer after it is written out
+        size = 0;
+        if (tid == 0) {
+            c->w[0] = 0;  // 0: nothing, 1: partial buffer only, 2: root
+            const bool ok = detail::ld_relaxed(&state->err) == 0 && lock(0, 0, BU::INUSE, kSiteLockPartial);
+            c->abort = !ok;
+            if (ok) {
+                const int bc = detail::ld_relaxed(&state->batchCount);
+                const int ps = detail::ld_relaxed(&state->partialBufferSize);
+                const int dc = detail::ld_relaxed(&state->deleteCount);
+                const int lim = detail::ld_relaxed(&state->outLimit);
+                c->bc = bc; c->ps = ps; c->dc = dc;
+                const int want = bc > 0 ? B : (PB ? ps : 0);
+                if (want == 0 || (sortOutput && dc + want > lim)) {
+                    unlock(0, 0);
+                } else if (bc == 0) {
+                    if (!check || __ldcg(node(0)) < threshold) c->w[0] = 1;
+                    else unlock(0, 0);
+                } else {
+                    if (bc > 1) detail::prefetch_l2(node(bc), nodeBytes());
+                    const bool ok1 = lock(1, 0, BU::INUSE, kSiteLockRoot);
+                    c->abort = !ok1;
+                    if (ok1 && check && !(__ldcg(node(1)) < threshold)) {
+                        unlock(1, 0);
+                        unlock(0, 0);
+                    } else if (ok1) {
+                        c->w[0] = 2;
+                        if (sortOutput) detail::st_relaxed(&state->deleteCount, dc + B);
+                        detail::st_relaxed(&state->batchCount, bc - 1);
+                        // take the last node (heap/buitdd/heap.cuh:372-378): atomicMax
+                        // takes it from AVAIL, INSHOLD or DELMOD
+                        bool okl = true;
+                        if (bc > 1) {
+                            unsigned long long t0 = 0;
+                            int prev;
+                            for (unsigned it = 0; (prev = detail::max_acquire(status + bc, BU::INUSE)) == BU::INUSE; ++it) {
+                                if (!keep_waiting(t0, it, kSiteLockLast, bc, prev)) { okl = false; break; }
+                            }
+                        }
+                        c->abort = !okl;
+                        if (okl) {
+                            const bool pb = PB && ps != 0 && bc > 1;
+                            op.issue((1u + (bc > 1 ? 1u : 0u) + (pb ? 1u : 0u)) * nodeBytes());
+                            load(R, 1, &c->bar);
+                            if (bc > 1) load(C, bc, &c->bar);
+                            if (pb) load(P, 0, &c->bar);
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const int mode = c->w[0];
+        const bool stop = c->abort || mode == 0;
+        const int bc = c->bc, ps = c->ps, dc = c->dc;
+        __syncthreads();  // every thread has read the control words before they change
+        if (stop) return;
+        K* out = items + (sortOutput ? dc : 0);
+        if (mode == 1) {
+            partial_out(out, ps, dc);
+            size = ps;
+            return;
+        }
+        if (!op.wait()) return;
+        smem_out(out, R, B);  // (:328-329)
+        size = B;
+        if (bc == 1) {  // the root was the only full node (:357-369)
+            __syncthreads();
+            if (tid == 0) { unlock(1, 0); unlock(0, 0); }
+            return;
+        }
+        fill_node(bc, B);  // reset the taken node (:396)
+        const bool pb = PB && ps != 0;
+        if (pb) merge(C, P, C, node(0));
+        __syncthreads();
+        if (tid == 0) {
+            fence();
+            setState(bc, 0);
+            setState(0, 0);
+        }
+        sift_loop(op, 1, 0, C, base + 2 * B, base + 3 * B);
+    }
+
+    // Block-wide copy of `count` keys from shared memory to dst.
+    __device__ __forceinline__ void smem_out(K* dst, const K* s, int count) const {
+        const int per = 16 / static_cast<int>(sizeof(K));
+        if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+            const int nv = count / per;
+            for (int q = threadIdx.x; q < nv; q += blockDim.x)
+                reinterpret_cast<uint4*>(dst)[q] = reinterpret_cast<const uint4*>(s)[q];
+            for (int q = nv * per + threadIdx.x; q < count; q += blockDim.x) dst[q] = s[q];
+        } else {
+            for (int q = threadIdx.x; q < count; q += blockDim.x) dst[q] = s[q];
+        }
+    }
+
     // The children of the node at one level, after they are locked and loaded.
     struct Level {
         int have, l, r, lPrev, rPrev, larger, smaller, lp, sp;
@@ -953,7 +1091,11 @@ struct Heap {
     __device__ __forceinline__ void order(Level& lv, const K* Xc, const K* Yc) const {
         lv.larger = lv.smaller = lv.lp = lv.sp = 0;
         if (lv.have != 3) return;
-        lv.larger = Xc[batchSize - 1] < Yc[batchSize - 1] ? lv.r : lv.l;
+        // the larger last key, the left child on a tie (tditdd_np :416), except
+        // when both end in init_limits: then the larger first key, so that a
+        // padded node's real keys never sink into a node past the heap
+        const K xl = Xc[batchSize - 1], yl = Yc[batchSize - 1];
+        lv.larger = (xl < yl || (xl == yl && !(xl < init_limits) && Xc[0] < Yc[0])) ? lv.r : lv.l;
         lv.smaller = lv.larger == lv.r ? lv.l : lv.r;
         lv.lp = lv.larger == lv.r ? lv.rPrev : lv.lPrev;
         lv.sp = lv.larger == lv.r ? lv.lPrev : lv.rPrev;

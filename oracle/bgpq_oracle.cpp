@@ -284,8 +284,17 @@ struct Model {
                 merge(sm.data(), node(l), node(cur), node(l));
                 return B;
             }
-            // two children (:479-531; bottom-up :421-479)
-            int larger = node(l)[B - 1] < node(r)[B - 1] ? r : l;
+            // two children (:479-531; bottom-up :421-479).  The larger child
+            // is the one with the larger last key, the left one on a tie
+            // (tditdd_np :416) -- except when both end in init_limits: then
+            // the one with the larger first key.  Otherwise a padded node
+            // (real keys, then init_limits) beside a node past the heap
+            // (all init_limits) counts as larger, and the carried batch with
+            // the padded node's real keys sinks into the node past the heap,
+            // where they are lost; the reference has that tie rule, without
+            // the exception.
+            const K ll = node(l)[B - 1], rl = node(r)[B - 1];
+            int larger = (ll < rl || (ll == rl && ll == init && node(l)[0] < node(r)[0])) ? r : l;
             int smaller = larger == r ? l : r;
             std::vector<K> low(B);
             merge(node(l), node(r), low.data(), node(larger));

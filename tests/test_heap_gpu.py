@@ -189,6 +189,32 @@ def test_heap_sort_ragged_sizes(B):
         assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("B,chunk", [(256, 256), (256, 100), (1024, 333)])
+def test_ragged_without_partial_buffer(variant, B, chunk):
+    """Without the partial buffer a short insert is padded with init_limits
+    and inserted as a full node; over many blocks every real key must come
+    out, in order, followed by the padding (a padded node beside a node past
+    the heap must not lose its keys)."""
+    for n in (20 * B + 37, 9 * B + 1, 33 * B - 5):
+        keys = pyoracle.gen("u32", n + chunk, "uniform", n)
+        inserts = (n + chunk - 1) // chunk
+        pad = inserts * B - n
+        total = n + pad
+        h = gh.Heap(batch_num_for(total, B), B, key="u32", variant=variant, partial_buffer=False)
+        h.set_grid(16)
+        h.insert(to_dev(keys, "u32"), chunk=chunk)
+        assert h.item_count() == total
+        out = empty_dev(total, "u32")
+        for step in range(3):  # a few single deletes, then the rest in bulk
+            assert h.delete_root(out) == B
+        assert h.delete(out) == total - 3 * B  # the bulk delete writes from out[0]
+        h.close()
+        want = np.concatenate([np.sort(keys), np.full(pad, 0xFFFFFFFF, np.uint32)])
+        got = to_host(out, "u32")
+        assert np.array_equal(got[:total - 3 * B], want[3 * B:]), (n, chunk)
+
+
 # test/heap_test.cu:120-171: insert half, concurrent insert + delete, delete the
 # rest.  Deletes that overlap inserts need not come out in global order, so
 # the bar is: no key lost or duplicated over the three phases, a valid heap

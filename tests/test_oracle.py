@@ -192,6 +192,83 @@ def test_model_heap_sort_random(variant, pb):
     assert np.array_equal(out[:n], np.sort(keys))
 
 
+def padded_sequence(seed, B=16):
+    """Full inserts of B keys plus one short insert at a random place: without
+    the partial buffer the short one is padded with init_limits and inserted
+    as a full node."""
+    rng = np.random.default_rng(seed)
+    nfull = int(rng.integers(3, 12))
+    tail = int(rng.integers(1, B))
+    keys = rng.integers(0, 2**32 - 1, nfull * B + tail, dtype=np.uint32)
+    pieces = [B] * nfull
+    pieces.insert(int(rng.integers(0, nfull + 1)), tail)
+    return keys, pieces, B - tail
+
+
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+def test_model_keeps_padded_keys(variant):
+    """A padded node whose sibling lies past the heap (all init_limits) ties
+    with it on the last key.  The larger child is then the one with the larger
+    first key, so the carried batch -- with the padded node's real keys --
+    stays inside the heap; every key comes out, in order."""
+    B = 16
+    for seed in range(200):
+        keys, pieces, pad = padded_sequence(seed, B)
+        m = pyoracle.Model("u32", variant, False, 1024, B)
+        pos = 0
+        for p in pieces:
+            assert m.insert(keys[pos:pos + p]) == 0
+            pos += p
+        out = np.zeros(len(keys) + pad + 4 * B, np.uint32)
+        while m.delete(out):
+            pass
+        want = np.concatenate([np.sort(keys), np.full(pad, 0xFFFFFFFF, np.uint32)])
+        assert np.array_equal(out[:len(want)], want), seed
+
+
+def test_reference_loses_padded_keys():
+    """The reference's tie rule (tditdd_np/heap.cuh:416: the left child on a
+    tie) loses the real keys of a padded node in the sequence below; the
+    model keeps them.  Runs only where oracle/_ref holds the reference's
+    heaps compiled for the host (built from the reference tree)."""
+    import ctypes
+    import os
+    lib_path = os.path.join(os.path.dirname(pyoracle.HERE), "oracle", "_ref", "libbgpq_ref.so")
+    if not os.path.exists(lib_path):
+        pytest.skip("reference heaps not built here")
+    ref = ctypes.CDLL(lib_path)
+    vp = ctypes.c_void_p
+
+    def fn(name, res=ctypes.c_int):
+        f = getattr(ref, f"tditdd_np_u32_{name}")
+        f.restype = res
+        return f
+
+    keys, pieces, pad = padded_sequence(28)
+    B = 16
+    create = fn("create", vp)
+    create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint32]
+    h = create(1024, B, 0xFFFFFFFF)
+    m = pyoracle.Model("u32", "topdown", False, 1024, B)
+    pos = 0
+    for p in pieces:
+        chunk = np.ascontiguousarray(keys[pos:pos + p])
+        pos += p
+        assert fn("insert")(vp(h), vp(chunk.ctypes.data), p) == 0
+        assert m.insert(chunk) == 0
+    n_out = len(keys) + pad
+    ref_out = np.zeros(n_out + 4 * B, np.uint32)
+    model_out = np.zeros(n_out + 4 * B, np.uint32)
+    sz = ctypes.c_int()
+    for _ in range(len(pieces) + 2):
+        assert fn("delete")(vp(h), vp(ref_out.ctypes.data), ctypes.byref(sz)) == 0
+        m.delete(model_out)
+    fn("destroy", None)(vp(h))
+    want = np.concatenate([np.sort(keys), np.full(pad, 0xFFFFFFFF, np.uint32)])
+    assert np.array_equal(model_out[:n_out], want)
+    assert not np.array_equal(np.sort(ref_out[:n_out]), want), "the reference kept every key here"
+
+
 def test_model_capacity():
     m = pyoracle.Model("u32", "topdown", False, 2, 16)
     k = np.arange(16, dtype=np.uint32)
