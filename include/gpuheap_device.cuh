@@ -1200,26 +1200,36 @@ struct Heap {
             }
             if (!op.wait()) return;
             order(lv, Xc, Yc);
-            if (lv.have == 3) {
-                merge(Xc, Yc, Xc, node(lv.larger));
-                __syncthreads();
-            }
-            // case analysis against the carried batch
             int done = 1, single = 0;
-            if (lv.have == 0) {  // no children (:452-460)
-                store_node(cur, C);
-            } else if (lv.have != 3) {  // one child (:461-477)
-                single = lv.have == 1 ? lv.l : lv.r;
-                merge(C, lv.have == 1 ? Xc : Yc, node(cur), node(single));
-            } else if (C[0] >= Xc[B - 1]) {
-                store_node(cur, Xc);  // the carried batch goes on unchanged
+            if (lv.have == 3 && !(C[0] < (Xc[B - 1] < Yc[B - 1] ? Xc[B - 1] : Yc[B - 1]))) {
+                // The carried batch starts at or above one child's last key, so
+                // at or above the B-th smallest key of the two children: the
+                // current node becomes the smaller half of the children and
+                // the carried batch goes on unchanged (the first case below),
+                // so the merge writes both halves straight to their nodes.
+                merge(Xc, Yc, node(cur), node(lv.larger));
                 done = 0;
-            } else if (VARIANT == kTopDown || !PB ? (C[B - 1] <= Xc[0]) : (C[B - 1] < Xc[0])) {  // buitdd alone uses < (:451)
-                store_node(cur, C);
-                store_node(lv.smaller, Xc);
             } else {
-                merge(C, Xc, node(cur), C);
-                done = 0;
+                if (lv.have == 3) {
+                    merge(Xc, Yc, Xc, node(lv.larger));
+                    __syncthreads();
+                }
+                // case analysis against the carried batch
+                if (lv.have == 0) {  // no children (:452-460)
+                    store_node(cur, C);
+                } else if (lv.have != 3) {  // one child (:461-477)
+                    single = lv.have == 1 ? lv.l : lv.r;
+                    merge(C, lv.have == 1 ? Xc : Yc, node(cur), node(single));
+                } else if (C[0] >= Xc[B - 1]) {
+                    store_node(cur, Xc);  // the carried batch goes on unchanged
+                    done = 0;
+                } else if (VARIANT == kTopDown || !PB ? (C[B - 1] <= Xc[0]) : (C[B - 1] < Xc[0])) {  // buitdd alone uses < (:451)
+                    store_node(cur, C);
+                    store_node(lv.smaller, Xc);
+                } else {
+                    merge(C, Xc, node(cur), C);
+                    done = 0;
+                }
             }
             __syncthreads();
             if (tid == 0) {
