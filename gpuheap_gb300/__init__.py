@@ -48,6 +48,7 @@ _SIGS = {
     "gh_heap_sync": (_I, [_VP, _VP]),
     "gh_heap_insert_batch": (_I, [_VP, _VP, _I, _VP]),
     "gh_heap_delete_batch": (_I, [_VP, _VP, ctypes.POINTER(_I), _VP]),
+    "gh_heap_retrieve": (_I, [_VP, _VP, _I, ctypes.POINTER(_I), _VP]),
     "gh_heap_sort": (_I, [_VP, _VP, _LL, _VP, _VP]),
     "gh_heap_check": (_I, [_VP, ctypes.POINTER(_I), ctypes.c_char_p, _I, _VP]),
     "gh_heap_item_count": (_I, [_VP, ctypes.POINTER(_LL)]),
@@ -281,6 +282,15 @@ class Heap:
         sz = _I()
         _check(lib().gh_heap_delete_batch(self._h, _ptr(items), ctypes.byref(sz), _stream(stream)), "deleteRoot")
         return sz.value
+
+    def retrieve(self, out, size, stream=None):
+        """retrieve(ret, *size) by one block (applications/sssp_longfei_new/
+        heap.cuh:79-270): the `size` smallest keys (at most one batch) into
+        out[0, n), ascending; returns n.  Heaps with the partial buffer."""
+        got = _I()
+        _check(lib().gh_heap_retrieve(self._h, _ptr(out), int(size), ctypes.byref(got), _stream(stream)),
+               "retrieve")
+        return got.value
 
     def insert(self, keys, n=None, chunk=0, stream=None):
         """Bulk insertion of n keys in insertion() calls of `chunk` keys over

@@ -28,6 +28,7 @@ struct gh_heap {
     int numSMs;
     gh::impl::CheckResult* check;  // device scratch for gh_heap_check
     int* opSize;                   // device word for gh_heap_delete_batch
+    void* scratch;                 // one batch of keys for gh_heap_retrieve
 };
 
 namespace {
@@ -182,6 +183,7 @@ gh_status gh_heap_create(gh_heap** out, int key_kind, int variant, int partial_b
     if (cudaMalloc(&h->d.state, sizeof(gh::HeapState)) != cudaSuccess) { cudaGetLastError(); return fail(GH_ERR_CUDA); }
     if (cudaMalloc(&h->check, sizeof(gh::impl::CheckResult)) != cudaSuccess) { cudaGetLastError(); return fail(GH_ERR_CUDA); }
     if (cudaMalloc(&h->opSize, sizeof(int)) != cudaSuccess) { cudaGetLastError(); return fail(GH_ERR_CUDA); }
+    if (cudaMalloc(&h->scratch, static_cast<size_t>(batch_size) * kb) != cudaSuccess) { cudaGetLastError(); return fail(GH_ERR_CUDA); }
     gh_status st = fill_items(h, nullptr);
     if (st != GH_OK) return fail(st);
     if (cudaDeviceSynchronize() != cudaSuccess) return fail(GH_ERR_CUDA);
@@ -196,6 +198,7 @@ gh_status gh_heap_destroy(gh_heap* h) {
     if (h->d.state) cudaFree(h->d.state);
     if (h->check) cudaFree(h->check);
     if (h->opSize) cudaFree(h->opSize);
+    if (h->scratch) cudaFree(h->scratch);
     delete h;
     return GH_OK;
 }
@@ -398,6 +401,23 @@ gh_status gh_heap_delete_batch(gh_heap* h, void* out_dev, int* size, void* strea
     GH_CUDA(cudaMemcpyAsync(&sz, h->opSize, sizeof(int), cudaMemcpyDeviceToHost, s));
     GH_CUDA(cudaStreamSynchronize(s));
     if (size) *size = sz;
+    return device_error(h);
+}
+
+gh_status gh_heap_retrieve(gh_heap* h, void* out_dev, int size, int* n_out, void* stream) {
+    if (!h || size < 0 || (size > 0 && !out_dev)) return GH_ERR_INVALID;
+    if (!h->d.pb) return GH_ERR_INVALID;  // the remainder goes back through the partial buffer
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const gh::impl::LaunchArgs a = args_of(h, s);
+    gh_status st = with_key(h, [&](auto k) {
+        using K = decltype(k);
+        return gh::impl::launch_retrieve<K>(a, static_cast<K*>(out_dev), size, static_cast<K*>(h->scratch));
+    });
+    if (st != GH_OK) return st;
+    int got = 0;
+    GH_CUDA(cudaMemcpyAsync(&got, h->opSize, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GH_CUDA(cudaStreamSynchronize(s));
+    if (n_out) *n_out = got;
     return device_error(h);
 }
 

@@ -96,6 +96,16 @@ __global__ void __launch_bounds__(1024) k_concurrent(H h, const K* __restrict__ 
     }
 }
 
+// One retrieve of up to `want` keys by one block; the count goes to *sizeOut.
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_retrieve(H h, K* out, int want, K* scratch, int* sizeOut) {
+    if constexpr (H::kHasPartialBuffer) {
+        int size = want;
+        h.retrieve(out, size, scratch, 0);
+        if (threadIdx.x == 0) *sizeOut = size;
+    }
+}
+
 // One delete by one block; the size goes to *sizeOut.
 template <typename H, typename K>
 __global__ void __launch_bounds__(1024) k_delete_one(H h, K* out, int* sizeOut) {

@@ -25,6 +25,8 @@ cudaError_t launch_erase(const LaunchArgs& a, K* out, const K* threshold = nullp
 template <typename K>
 cudaError_t launch_erase_one(const LaunchArgs& a, K* out);
 template <typename K>
+cudaError_t launch_retrieve(const LaunchArgs& a, K* out, int want, K* scratch);
+template <typename K>
 cudaError_t launch_insert_counted(const LaunchArgs& a, const K* keys, const unsigned long long* n, int chunk);
 template <typename K>
 cudaError_t launch_concurrent(const LaunchArgs& a, const K* keys, long long n, int chunk, K* out, long long deletes);
@@ -150,6 +152,20 @@ cudaError_t launch_erase_one(const LaunchArgs& a, K* out) {
 }
 
 template <typename K>
+cudaError_t launch_retrieve(const LaunchArgs& a, K* out, int want, K* scratch) {
+    return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
+        using H = decltype(proto);
+        const H h = view_of<H>(*a.d, 0);  // outputs at scratch[0]
+        const size_t smem = H::smemBytes(a.d->batchSize);
+        cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_retrieve<H, K>), smem);
+        if (e != cudaSuccess) return e;
+        k_retrieve<H, K><<<1, a.threads, smem, a.stream>>>(h, out, want, scratch, a.opSize);
+        count_launch();
+        return cudaGetLastError();
+    });
+}
+
+template <typename K>
 void device_view(const Desc& d, void* out, size_t* bytes) {
     auto put = [&](auto proto) {
         using H = decltype(proto);
@@ -166,6 +182,7 @@ void device_view(const Desc& d, void* out, size_t* bytes) {
     template cudaError_t launch_erase<K>(const LaunchArgs&, K*, const K*);                       \
     template cudaError_t launch_insert_counted<K>(const LaunchArgs&, const K*, const unsigned long long*, int); \
     template cudaError_t launch_erase_one<K>(const LaunchArgs&, K*);                             \
+    template cudaError_t launch_retrieve<K>(const LaunchArgs&, K*, int, K*);                     \
     template cudaError_t launch_concurrent<K>(const LaunchArgs&, const K*, long long, int, K*, long long); \
     template void device_view<K>(const Desc&, void*, size_t*);
 #endif  // GH_INSTANTIATE

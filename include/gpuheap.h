@@ -114,6 +114,14 @@ gh_status gh_heap_insert_batch(gh_heap* h, const void* keys_dev, int size, void*
  * gh_heap_reset sets it back to 0.  Synchronizes the stream; *size = keys written. */
 gh_status gh_heap_delete_batch(gh_heap* h, void* out_dev, int* size, void* stream);
 
+/* retrieve(ret, *size) (applications/sssp_longfei_new/heap.cuh:79-270) by
+ * one thread block: the `size` smallest keys -- at most batch_size, fewer
+ * when the heap holds fewer -- into out_dev[0, *n_out), ascending.  A delete
+ * takes the root batch, the rest of it goes back in through the partial
+ * buffer, so heaps without the partial buffer get GH_ERR_INVALID.
+ * Synchronizes the stream. */
+gh_status gh_heap_retrieve(gh_heap* h, void* out_dev, int size, int* n_out, void* stream);
+
 /* The plain heap-sort (test/partial_heap_test.cu:88-176, without the
  * concurrent phase): reset, insert in_dev[0, n) in batch_size calls, then
  * delete everything into out_dev[0, n).  out_dev must hold n keys. */

@@ -8,6 +8,8 @@
 //     heap.deleteRoot(items, size)              (heap/tditdd/heap.cuh:267)
 //     heap.deleteRoot(items, size, threshold)   (artifacts/astar/BGPQ_B/heap.cuh:260)
 //     heap.deleteUpdate(smemOffset)             (heap/tditdd/heap.cuh:345)
+//     heap.retrieve(ret, size, scratch, smemOffset)
+//                                               (applications/sssp_longfei_new/heap.cuh:79)
 // with the reference's meaning: operations are block-collective, a heap node
 // is a sorted batch of batchSize keys, node 0 is the partial buffer, and
 // `smemOffset` counts 4-byte words of dynamic shared memory reserved by the
@@ -329,6 +331,7 @@ struct Heap {
     // Four node buffers in shared memory: the carried batch (or insert
     // batch), the partial buffer (or loaded node) and the two children.
     static constexpr int kBufs = 4;
+    static constexpr bool kHasPartialBuffer = PB;
     static __host__ __device__ size_t smemBytes(int bs) {
         return kBufs * static_cast<size_t>(bs) * sizeof(K) + sizeof(OpCtl) + 16;
     }
@@ -1068,6 +1071,30 @@ struct Heap {
             setState(0, 0);
         }
         sift_loop(op, 1, 0, C, base + 2 * B, base + 3 * B);
+    }
+
+    // ------------------------------------------------------------------ retrieve
+    // retrieve(ret, *size) (applications/sssp_longfei_new/heap.cuh:79-270):
+    // the `size` smallest keys -- at most one batch, fewer when the heap holds
+    // fewer -- into ret[0, size), ascending; `size` returns the count.  Built
+    // from this heap's own operations: a delete takes the root (the B
+    // smallest keys) into `scratch`, the first `size` go to ret and the rest
+    // are inserted back, where they join the partial buffer, so no padding
+    // enters the heap.  `scratch` holds batchSize keys (global or shared,
+    // 16-byte aligned) outside the heap's shared-memory region; ret may not
+    // overlap it.  Outputs at scratch[0] need a view with sortOutput = 0.
+    // Heaps with the partial buffer only (the reference's retrieving heap
+    // has one).
+    __device__ __forceinline__ void retrieve(K* ret, int& size, K* scratch, int smemOffset) const {
+        static_assert(PB, "retrieve needs the partial buffer");
+        const int want = size < 0 ? 0 : size;
+        int got = 0;
+        if (want > 0) deleteMin(scratch, got, smemOffset);
+        const int take = got < want ? got : want;
+        for (int i = threadIdx.x; i < take; i += blockDim.x) ret[i] = scratch[i];
+        __syncthreads();
+        if (got > take) insertion(scratch + take, got - take, smemOffset);
+        size = take;
     }
 
     // Block-wide copy of `count` keys from shared memory to dst.

@@ -126,6 +126,81 @@ def test_random_ops_match_model(variant, pb, key, B, threads):
     h.close()
 
 
+def model_retrieve(m, size, B, dtype):
+    """The oracle side of retrieve: a delete of the root batch, the first
+    `size` keys returned, the rest inserted back."""
+    _, counters = m.state()
+    before = int(counters[2])
+    buf = np.zeros(before + 2 * B, dtype)
+    n = m.delete(buf)
+    keys = buf[before:before + n].copy()
+    take = min(n, size)
+    if n > take:
+        assert m.insert(keys[take:]) == 0
+    return keys[:take]
+
+
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("key,B", [("u32", 256), ("u64", 512), ("i32", 1024)])
+def test_retrieve_matches_model(variant, key, B):
+    """retrieve(ret, size): random inserts and retrieves of random sizes by one
+    block against the oracle (delete the root batch, return the first `size`,
+    insert the rest back): every retrieved run and the final heap bit-exact."""
+    rng = np.random.default_rng(B + len(variant))
+    n = 30 * B
+    bn = batch_num_for(n, B)
+    keys = pyoracle.gen(key, int(rng.integers(1 << 30)), "uniform", n)
+    h = gh.Heap(bn, B, key=key, variant=variant, partial_buffer=True)
+    m = pyoracle.Model(key, variant, True, bn, B)
+    dk = to_dev(keys, key)
+    out_d = empty_dev(B, key)
+    pos, got_total = 0, 0
+    while True:
+        if pos < n and rng.random() < 0.55:
+            s = min(int(rng.integers(1, B + 1)), n - pos)
+            h.insertion(dk[pos:pos + s], s)
+            assert m.insert(keys[pos:pos + s]) == 0
+            pos += s
+        else:
+            size = int(rng.integers(1, B + 1)) if rng.random() < 0.8 else B
+            got = h.retrieve(out_d, size)
+            want = model_retrieve(m, size, B, NP_KEY[key])
+            assert got == len(want)
+            assert np.array_equal(to_host(out_d, key)[:got], want)
+            got_total += got
+            if pos >= n and got == 0:
+                break
+    assert got_total == n
+    items, status, counters = h.snapshot()
+    mi, mc = m.state()
+    assert np.array_equal(items, mi)
+    assert np.array_equal(counters[:2], mc[:2])
+    h.close()
+
+
+def test_retrieve_edges():
+    B = 64
+    h = gh.Heap(16, B, key="u32", variant="bottomup", partial_buffer=True)
+    out = empty_dev(B, "u32")
+    assert h.retrieve(out, 10) == 0                     # empty heap
+    keys = np.arange(100, 100 + 3 * B + 5, dtype=np.uint32)[::-1].copy()
+    h.insert(to_dev(keys, "u32"), chunk=7)
+    assert h.retrieve(out, 0) == 0
+    assert h.retrieve(out, 5) == 5
+    assert np.array_equal(to_host(out, "u32")[:5], np.arange(100, 105))
+    assert h.retrieve(out, 10 * B) == B                   # at most one batch
+    assert np.array_equal(to_host(out, "u32"), np.arange(105, 105 + B))
+    assert h.item_count() == 3 * B + 5 - 5 - B
+    ok, msg = h.check_insert_heap()
+    assert ok, msg
+    h.close()
+    h = gh.Heap(16, B, key="u32", variant="topdown", partial_buffer=False)
+    with pytest.raises(gh.HeapError) as e:
+        h.retrieve(out, 5)
+    assert e.value.status == gh.GH_ERR_INVALID
+    h.close()
+
+
 def run_heap_sort(key, variant, pb, B, n, dist="uniform", seed=1, chunk=None, grid=0):
     keys = pyoracle.gen(key, seed, dist, n)
     h = gh.Heap(batch_num_for(n, B), B, key=key, variant=variant, partial_buffer=pb)
