@@ -70,6 +70,8 @@ _SIGS = {
     "gh_batch_destroy": (_I, [_VP]),
     "gh_batch_set_timeout": (_I, [_VP, ctypes.c_double]),
     "gh_batch_set_astar_blocks": (_I, [_VP, _LL, _I]),
+    "gh_batch_set_knapsack_order": (_I, [_VP, _I, _I]),
+    "gh_batch_knapsack_switches": (_I, [_VP, _VP, _VP]),
     "gh_batch_add_astar": (_I, [_VP, _I, _I, _VP, ctypes.POINTER(_I)]),
     "gh_batch_add_knapsack": (_I, [_VP, _I, _VP, _VP, _LL, ctypes.POINTER(_I)]),
     "gh_batch_build": (_I, [_VP, _VP]),

@@ -21,6 +21,7 @@ ASTAR, KNAPSACK = 0, 1
 PERSISTENT, GRAPH, PLAIN = 0, 1, 2
 _MODES = {"persistent": PERSISTENT, "graph": GRAPH, "plain": PLAIN}
 _VARIANTS = {"topdown": 0, "bottomup": 1}
+KNAPSACK_ORDERS = {"heap": 0, "fifo": 1, "switch": 2}
 
 
 def gen_grid(side, seed, obstacle_per_mille=200, height=None):
@@ -61,7 +62,7 @@ class Batch:
     """A set of searches uploaded once and run any number of times."""
 
     def __init__(self, instances, batch_size=256, variant="bottomup", block_threads=0, astar_cells_per_block=1 << 18,
-                 astar_max_blocks=8, timeout=2.0, stream=None):
+                 astar_max_blocks=8, timeout=2.0, stream=None, knapsack_order="heap", switch_counter=20):
         h = _VP()
         _check(lib().gh_batch_create(ctypes.byref(h), batch_size, _VARIANTS[variant], block_threads), "batch_create")
         self._h = h
@@ -71,6 +72,8 @@ class Batch:
             _check(lib().gh_batch_set_timeout(h, float(timeout)), "batch_set_timeout")
             _check(lib().gh_batch_set_astar_blocks(h, int(astar_cells_per_block), int(astar_max_blocks)),
                    "batch_set_astar_blocks")
+            _check(lib().gh_batch_set_knapsack_order(h, KNAPSACK_ORDERS[knapsack_order], int(switch_counter)),
+                   "batch_set_knapsack_order")
             for kind, data in instances:
                 if kind == "astar":
                     g = np.ascontiguousarray(data, np.uint8)
@@ -102,6 +105,12 @@ class Batch:
         if check:
             _check(rc, "batch_results")
         return res, st, stats
+
+    def knapsack_switches(self, stream=None):
+        """Heap/FIFO switches per instance in the last run (knapsack, order "switch")."""
+        out = np.zeros(len(self.kinds), np.int32)
+        _check(lib().gh_batch_knapsack_switches(self._h, out.ctypes.data, _stream(stream)), "knapsack_switches")
+        return out
 
     def info(self):
         c, t, g, th, ab = _I(), _I(), _I(), _I(), _LL()

@@ -58,6 +58,7 @@ struct gh_batch {
     long long timeoutNs = 2000000000LL;
     long long astarCellsPerBlock = 1 << 18;
     int astarMaxBlocks = 8;
+    int knapOrder = GH_KNAP_HEAP, switchCounter = 20;
     int device = 0, numSMs = 0;
     std::vector<HostInst> host;
     // device
@@ -151,6 +152,14 @@ gh_status gh_batch_set_astar_blocks(gh_batch* b, long long cells_per_block, int 
     return GH_OK;
 }
 
+gh_status gh_batch_set_knapsack_order(gh_batch* b, int order, int switch_counter) {
+    if (!b || order < GH_KNAP_HEAP || order > GH_KNAP_SWITCH || switch_counter < 1) return GH_ERR_INVALID;
+    b->knapOrder = order;
+    b->switchCounter = switch_counter;
+    if (b->built) free_device(b);
+    return GH_OK;
+}
+
 gh_status gh_batch_set_timeout(gh_batch* b, double seconds) {
     if (!b || !(seconds > 0) || seconds > 60.0) return GH_ERR_INVALID;
     b->timeoutNs = static_cast<long long>(seconds * 1e9);
@@ -218,7 +227,7 @@ gh_status gh_batch_build(gh_batch* b, void* stream) {
     const int B = b->batchSize;
     const int count = static_cast<int>(b->host.size());
     // sizes
-    struct Lay { size_t items, status, state, cost, g, w, p, W, P, pool, freeList; int bn, poolCap; };
+    struct Lay { size_t items, status, state, cost, g, w, p, W, P, pool, freeList, ring, fifo; int bn, poolCap; unsigned long long ringCap; };
     std::vector<Lay> lay(count);
     size_t off = align_up(sizeof(Inst) * count, 256);
     size_t tasksOff = 0, nextOff = 0;
@@ -236,6 +245,10 @@ gh_status gh_batch_build(gh_batch* b, void* stream) {
             // batched branch-and-bound explores far more nodes than a
             // sequential one; pool slots must fit the key's 20 bits
             keys = std::min<long long>(1LL << 19, std::max<long long>({1LL << 16, 64LL * B, 256LL * static_cast<long long>(h.w.size())}));
+            // a breadth-first frontier can be far wider: the FIFO orders get
+            // the largest pool the key's slot bits allow, and a heap that can
+            // take every pooled node back at a switch
+            if (b->knapOrder != GH_KNAP_HEAP) keys = 1LL << kSlotBits;
         }
         L.bn = heap_nodes(keys, B);
         L.state = off; off = align_up(off + sizeof(gh::HeapState), 256);
@@ -247,13 +260,22 @@ gh_status gh_batch_build(gh_batch* b, void* stream) {
             L.g = off; off = align_up(off + cells * 4, 256);
         } else {
             const int n = static_cast<int>(h.w.size());
-            L.poolCap = std::min((L.bn + 1) * B + 4 * B, 1 << kSlotBits);
+            L.poolCap = b->knapOrder != GH_KNAP_HEAP ? (1 << kSlotBits) : std::min((L.bn + 1) * B + 4 * B, 1 << kSlotBits);
             L.w = off; off = align_up(off + n * 4, 256);
             L.p = off; off = align_up(off + n * 4, 256);
             L.W = off; off = align_up(off + (n + 1) * 8, 256);
             L.P = off; off = align_up(off + (n + 1) * 8, 256);
             L.pool = off; off = align_up(off + static_cast<size_t>(L.poolCap) * 16, 256);
             L.freeList = off; off = align_up(off + static_cast<size_t>(L.poolCap + B) * 4, 256);
+            L.ringCap = 0;
+            if (b->knapOrder != GH_KNAP_HEAP) {
+                // every live node holds a pool slot, so a ring of the pool's
+                // size takes all of them at a switch
+                L.ringCap = 1;
+                while (L.ringCap < static_cast<unsigned long long>(L.poolCap)) L.ringCap <<= 1;
+                L.fifo = off; off = align_up(off + sizeof(gh::FifoState), 256);
+                L.ring = off; off = align_up(off + static_cast<size_t>(L.ringCap) * 8, 256);
+            }
         }
     }
     // task order: largest instances first, each instance's blocks together
@@ -317,6 +339,13 @@ gh_status gh_batch_build(gh_batch* b, void* stream) {
             d.pool = reinterpret_cast<int4*>(A + L.pool);
             d.freeList = reinterpret_cast<int*>(A + L.freeList);
             d.greedy = h.greedy;
+            d.order = b->knapOrder;
+            d.switchCounter = b->switchCounter;
+            if (L.ringCap) {
+                d.ring = reinterpret_cast<u64*>(A + L.ring);
+                d.fifo = reinterpret_cast<gh::FifoState*>(A + L.fifo);
+                d.ringCap = L.ringCap;
+            }
             if (cudaMemcpyAsync(A + L.w, h.w.data(), n * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
                 cudaMemcpyAsync(A + L.p, h.p.data(), n * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
                 cudaMemcpyAsync(A + L.W, h.W.data(), (n + 1) * 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
@@ -389,6 +418,17 @@ gh_status gh_batch_results(gh_batch* b, long long* results, int* status, unsigne
         if (d.failed && worst == GH_OK) worst = static_cast<gh_status>(d.failed);
     }
     return worst;
+}
+
+gh_status gh_batch_knapsack_switches(gh_batch* b, int* switches, void* stream) {
+    if (!b || !b->built || !switches) return GH_ERR_INVALID;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int count = static_cast<int>(b->host.size());
+    if (cudaMemcpyAsync(b->hinst.data(), b->insts, sizeof(Inst) * count, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return GH_ERR_CUDA;
+    for (int i = 0; i < count; ++i) switches[i] = b->hinst[i].kind == GH_SEARCH_KNAPSACK ? b->hinst[i].switches : 0;
+    return GH_OK;
 }
 
 gh_status gh_batch_info(gh_batch* b, int* count, int* tasks, int* grid, int* threads, long long* arena_bytes) {

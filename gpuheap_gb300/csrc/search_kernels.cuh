@@ -22,6 +22,14 @@
 //     item keeps the parent's bound, so many nodes tie; deepest first reaches
 //     good incumbents early, as a sequential best-first search does.
 //
+// Knapsack instances can also run the reference's other two models on the
+// same node pool: breadth-first through a FIFO ring (models_fifo.cuh:13-112,
+// gh::Fifo) and the heap/FIFO switch (models.cuh:23-440): heap mode until
+// `switchCounter` batches in a row insert children without raising the best
+// profit, FIFO mode until that many batches in a row raise it; at a switch
+// every live node moves across and nodes that can no longer beat the best
+// are dropped (the reference's invalidFilter between modes).
+//
 // Blocks find work through a task list: an instance appears once per block
 // it should get (large grids several times, knapsacks once), largest first;
 // blocks of one instance share its heap and stop by the protocol of
@@ -32,6 +40,7 @@
 #include <climits>
 
 #include "gpuheap.h"
+#include "gpuheap_fifo.cuh"
 #include "heap_launch.cuh"
 #include "sssp_relax.cuh"
 #include "worklist.cuh"
@@ -84,6 +93,14 @@ struct alignas(16) Inst {
     int greedy;  // knapsack: profit of the greedy fill (first incumbent)
     int done;    // the search has finished (heap empty, no block inside)
     unsigned long long reached, distSum;  // SSSP: reachable vertices, sum of their distances
+    // knapsack FIFO / switch models (ring == NULL: heap only)
+    u64* ring;                  // ringCap keys, a power of two
+    gh::FifoState* fifo;
+    unsigned long long ringCap;
+    int order;                  // GH_KNAP_HEAP / GH_KNAP_FIFO / GH_KNAP_SWITCH
+    int switchCounter;          // batches in a row that trigger a switch
+    int mode;                   // structure in use: 0 heap, 1 FIFO
+    int switches;               // mode changes so far
 };
 
 // Prune thresholds (the app_t_val of deleteRoot, artifacts/astar/BGPQ_B/
@@ -151,6 +168,10 @@ __global__ void k_search_fill(Inst* insts, const int* ids, int B) {
                                                          : static_cast<size_t>(in->nv);
         for (size_t q = first; q < cells; q += stride) in->g[q] = 0xffffffffu;
     }
+    if (in->fifo) {
+        unsigned long long* w = reinterpret_cast<unsigned long long*>(in->fifo);
+        for (size_t q = first; q < sizeof(gh::FifoState) / 8; q += stride) w[q] = 0;
+    }
 }
 
 // Counters, incumbent and the seed key in the partial buffer (after the
@@ -200,8 +221,16 @@ __global__ void k_search_seed(Inst* insts, const int* ids, int count) {
             long long b = in->P[lo];
             if (lo < in->n) b += (in->cap - in->W[lo]) * in->p[lo] / in->w[lo];
             const bool live = b > in->greedy;
-            if (live) in->items[0] = knap_key(b, 0, 0);
-            st->partialBufferSize = live ? 1 : 0;
+            in->mode = in->order == GH_KNAP_FIFO ? 1 : 0;
+            in->switches = 0;
+            if (in->mode == 1) {  // breadth-first: the root node goes into the ring
+                if (live) in->ring[0] = knap_key(b, 0, 0);
+                in->fifo->end = in->fifo->write = live ? 1 : 0;
+                st->partialBufferSize = 0;
+            } else {
+                if (live) in->items[0] = knap_key(b, 0, 0);
+                st->partialBufferSize = live ? 1 : 0;
+            }
         }
     }
 }
@@ -240,6 +269,73 @@ __device__ __forceinline__ void flush_rest(const H& heap, u64* emit, int* cnt, i
     __syncthreads();
     if (threadIdx.x == 0) *cnt = 0;
     __syncthreads();
+}
+
+// Pushes the emitted keys into the ring.  One block owns the ring, so
+// nothing frees slots while it pushes: a push that would not fit sets
+// *overflow (the instance then fails with GH_ERR_CAPACITY) instead of
+// waiting for room.
+__device__ __forceinline__ void fifo_flush(const gh::Fifo<u64>& f, u64* emit, int* cnt, int* overflow,
+                                           unsigned long long& inserted) {
+    __syncthreads();
+    const int c = *cnt;
+    if (c > 0) {
+        if (threadIdx.x == 0 && f.state->end - f.state->begin + static_cast<unsigned long long>(c) > f.capacity)
+            *overflow = 1;
+        __syncthreads();
+        if (!*overflow) f.push(emit, c);
+        inserted += c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *cnt = 0;
+    __syncthreads();
+}
+
+// Switch to the FIFO (models.cuh:358-372, heapDataToArray): every node's keys
+// below the prune threshold -- a prefix, nodes are sorted -- go into the
+// ring, and the heap is emptied.  The block owns the heap (one block per
+// knapsack instance) and no key of it is in flight.
+template <typename H>
+__device__ void heap_to_fifo(const H& heap, const gh::Fifo<u64>& f, u64 threshold, int* ctl) {
+    gh::HeapState* st = heap.state;
+    const int bc = st->batchCount, ps = st->partialBufferSize;
+    const int B = heap.batchSize;
+    for (int i = 0; i <= bc; ++i) {
+        u64* nd = reinterpret_cast<u64*>(heap.heapItems) + static_cast<size_t>(i) * B;
+        const int len = i == 0 ? ps : B;
+        if (threadIdx.x == 0) ctl[7] = 0;
+        __syncthreads();
+        int c = 0;
+        for (int j = threadIdx.x; j < len; j += blockDim.x) c += nd[j] < threshold ? 1 : 0;
+        if (c) atomicAdd(&ctl[7], c);
+        __syncthreads();
+        const int keep = ctl[7];
+        if (keep > 0) f.push(nd, keep);  // fits: the ring is at least the node pool, one slot per live key
+        for (int j = threadIdx.x; j < B; j += blockDim.x) nd[j] = ~0ull;
+        if (threadIdx.x == 0) heap.status[i] = 0;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        st->batchCount = 0;
+        st->partialBufferSize = 0;
+    }
+    __syncthreads();
+}
+
+// Switch back to the heap (models.cuh:262-280): the ring's keys are
+// inserted in batches.
+template <typename H>
+__device__ void fifo_to_heap(const H& heap, const gh::Fifo<u64>& f, u64* batch, int heapOff) {
+    const int B = heap.batchSize;
+    for (;;) {
+        const typename gh::Fifo<u64>::Claim c = f.claim(B);
+        if (c.n == 0) break;
+        f.copy_out(c, batch);
+        f.release(c);
+        __syncthreads();
+        heap.insertion(reinterpret_cast<typename H::key_type*>(batch), c.n, heapOff);
+        if (heap.failed()) break;
+    }
 }
 
 template <typename H>
@@ -333,11 +429,27 @@ __device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int h
     unsigned long long pops = 0, expanded = 0, inserted = 0, waitStart = 0;
     int lastBusy = -1, batches = 0;
     const KnapThreshold prune{best};
+    const gh::Fifo<u64> fifo{in->ring, in->fifo, in->ringCap, heap.timeoutNs};
+    int mode = in->mode;               // block-uniform: 0 heap, 1 FIFO
+    int counter = 0, prevBest = 0;     // switch model, thread 0
+    if (tid == 0) prevBest = __ldcg(best);
     for (;;) {
         if (maxBatches && batches++ == maxBatches) break;
-        if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
         int size = 0;
-        heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap), heapOff);
+        if (mode == 0) {
+            if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
+            heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap), heapOff);
+        } else {
+            // breadth-first (models_fifo.cuh:46-52): the oldest batch of the ring;
+            // the search is over when the ring is empty (one block owns it)
+            if (__syncthreads_or(threadIdx.x == 0 && gh::detail::ld_relaxed(&in->stop) != 0)) break;
+            const typename gh::Fifo<u64>::Claim c = fifo.claim(B);
+            if (c.n == 0) break;
+            fifo.copy_out(c, batch);
+            fifo.release(c);
+            size = c.n;
+        }
+        const unsigned long long insertedBefore = inserted;
         pops += size;
         // read the popped nodes, then return their slots
         constexpr unsigned kSlotMask = (1u << kSlotBits) - 1;
@@ -382,14 +494,39 @@ __device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int h
             }
             __syncthreads();
             if (tid == 0 && ctl[3] < 0) ctl[3] = 0;
-            flush_full(heap, emit, &ctl[1], B, heapOff, inserted);
+            if (mode == 0) flush_full(heap, emit, &ctl[1], B, heapOff, inserted);
+            else fifo_flush(fifo, emit, &ctl[1], &ctl[5], inserted);
         }
-        flush_rest(heap, emit, &ctl[1], heapOff, inserted);
-        if (ctl[5]) {  // node pool exhausted
+        if (mode == 0) flush_rest(heap, emit, &ctl[1], heapOff, inserted);
+        else fifo_flush(fifo, emit, &ctl[1], &ctl[5], inserted);
+        if (ctl[5]) {  // node pool or ring exhausted
             if (tid == 0) { in->failed = GH_ERR_CAPACITY; gh::detail::st_relaxed(&in->stop, 1); }
         }
-        gh::app::batch_done(heap.state);
-        if (heap.failed() || ctl[5]) break;
+        if (mode == 0) gh::app::batch_done(heap.state);
+        if (heap.failed() || ctl[5] || __syncthreads_or(threadIdx.x == 0 && in->fifo != nullptr && fifo.failed())) break;
+        if (in->order == GH_KNAP_SWITCH) {
+            // models.cuh:102-117 (FIFO) and :210-227 (heap): count batches in
+            // a row that inserted children with the best profit unchanged
+            // (heap mode) or raised (FIFO mode)
+            if (tid == 0) {
+                const int nb = __ldcg(best);
+                const bool ins = inserted > insertedBefore;
+                counter = (ins && (mode == 0 ? nb == prevBest : nb > prevBest)) ? counter + 1 : 0;
+                prevBest = nb;
+                ctl[6] = counter >= in->switchCounter ? 1 : 0;
+                if (ctl[6]) counter = 0;
+            }
+            __syncthreads();
+            const int flip = ctl[6];
+            __syncthreads();
+            if (flip) {
+                if (mode == 0) heap_to_fifo(heap, fifo, prune(heap), ctl);
+                else fifo_to_heap(heap, fifo, batch, heapOff);
+                mode ^= 1;
+                if (tid == 0) { in->mode = mode; in->switches += 1; }
+                if (heap.failed()) break;
+            }
+        }
     }
     if (tid == 0) {
         in->freeTop = ctl[3];
@@ -477,7 +614,9 @@ __global__ void k_search_collect(Inst* insts, const int* ids, int final, int bat
             in->failed = err == gh::kErrCapacity ? GH_ERR_CAPACITY : err == gh::kErrTimeout ? GH_ERR_TIMEOUT : GH_ERR_STATE;
         const int bc = in->state->batchCount;
         const bool empty = bc == 0 && in->state->partialBufferSize == 0;
-        const bool finished = empty || in->items[bc > 0 ? batchSize : 0] >= prune_threshold(in);
+        const bool ringEmpty = in->fifo == nullptr || in->fifo->end == in->fifo->begin;
+        const bool finished = (empty || in->items[bc > 0 ? batchSize : 0] >= prune_threshold(in)) && ringEmpty;
+        if (in->fifo && in->fifo->err && !in->failed) in->failed = GH_ERR_TIMEOUT;
         if (final && !in->failed && !finished && !in->stop) in->failed = GH_ERR_STATE;
         in->done = in->failed || in->stop || finished;
         s_done = in->done && !in->failed && in->kind == GH_SEARCH_SSSP;

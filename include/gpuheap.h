@@ -228,6 +228,10 @@ gh_status gh_sssp(gh_heap* h, int n, const long long* rowptr_dev, const int* col
 typedef struct gh_batch gh_batch;
 typedef enum { GH_SEARCH_ASTAR = 0, GH_SEARCH_KNAPSACK = 1, GH_SEARCH_SSSP = 2 } gh_search_kind;
 typedef enum { GH_BATCH_PERSISTENT = 0, GH_BATCH_GRAPH = 1, GH_BATCH_PLAIN = 2 } gh_batch_mode;
+/* The knapsack search order (artifacts/knapsack/main.cu:100-130 models):
+ * best-first on the heap (models_pq.cuh), breadth-first through a FIFO
+ * ring (models_fifo.cuh), or the heap/FIFO switch (models.cuh:241-440). */
+typedef enum { GH_KNAP_HEAP = 0, GH_KNAP_FIFO = 1, GH_KNAP_SWITCH = 2 } gh_knapsack_order;
 
 /* batch_size: power of two in [32, 1024]; block_threads 0 (= min(batch_size,
  * 512)), batch_size or batch_size / 2, at most 512. */
@@ -239,6 +243,16 @@ gh_status gh_batch_set_timeout(gh_batch* b, double seconds);
  * max(1, cells / cells_per_block)) blocks (default 2^18 cells, 8 blocks);
  * knapsack instances get one. */
 gh_status gh_batch_set_astar_blocks(gh_batch* b, long long cells_per_block, int max_blocks);
+/* Search order of every knapsack instance of the batch (default
+ * GH_KNAP_HEAP); for GH_KNAP_SWITCH, `switch_counter` batches in a row
+ * (> 0; the reference uses 20) that insert children without raising the
+ * best profit move the nodes from the heap to the FIFO, and as many that
+ * raise it move them back.  The FIFO orders give each knapsack instance a
+ * ring of at least its node pool.  Takes effect at the next build. */
+gh_status gh_batch_set_knapsack_order(gh_batch* b, int order, int switch_counter);
+/* Heap/FIFO switches each knapsack instance made in the last run (0 for
+ * other instances); switches_host holds one int per instance. */
+gh_status gh_batch_knapsack_switches(gh_batch* b, int* switches_host, void* stream);
 /* Grid A*: cost_host[y * width + x] in 1..9 is the cost of entering the cell,
  * 0 an obstacle; the search runs from (0, 0) to (width-1, height-1) with the
  * Manhattan heuristic (artifacts/astar/astar_map.cuh:137-138 keeps start and

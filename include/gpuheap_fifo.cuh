@@ -60,49 +60,66 @@ __device__ __forceinline__ unsigned long long now() {
     return t;
 }
 
+// Loads of a copy's source: through L2 (__ldcg) from global memory -- ring
+// slots are rewritten every lap and must not be served from a stale L1 line
+// -- and plain loads from shared memory, which __ldcg cannot address.
+template <bool kGlobal, typename T>
+__device__ __forceinline__ T load_src(const T* p) {
+    if constexpr (kGlobal) return __ldcg(p);
+    else return *p;
+}
+
 // Copy of n keys by T threads, this one being thread t (a block or the whole
 // grid).  When source and destination share their offset within 16 bytes
 // the body moves as 16-byte vectors, four per thread in flight; otherwise
-// four scalar keys per thread are loaded before they are stored.  Source loads go through L2 (__ldcg): ring slots are rewritten
-// every lap and must not be served from a stale L1 line.
-template <typename K>
-__device__ __forceinline__ void copy_keys(K* __restrict__ dst, const K* __restrict__ src, long long n, long long t,
-                                          long long T) {
+// four scalar keys per thread are loaded before they are stored.
+template <bool kGlobal, typename K>
+__device__ __forceinline__ void copy_keys_from(K* __restrict__ dst, const K* __restrict__ src, long long n, long long t,
+                                               long long T) {
     constexpr int kVec = 16 / sizeof(K);
     const uintptr_t d = reinterpret_cast<uintptr_t>(dst), s = reinterpret_cast<uintptr_t>(src);
     if (((d ^ s) & 15) == 0 && n >= 4 * kVec) {
         const long long head = static_cast<long long>(((16 - (d & 15)) & 15) / sizeof(K));
-        if (t < head) dst[t] = __ldcg(src + t);
+        if (t < head) dst[t] = load_src<kGlobal>(src + t);
         const long long nv = (n - head) / kVec;
         uint4* dv = reinterpret_cast<uint4*>(dst + head);
         const uint4* sv = reinterpret_cast<const uint4*>(src + head);
         long long i = t;
 #pragma unroll 1
         for (; i + 3 * T < nv; i += 4 * T) {
-            const uint4 a = __ldcg(sv + i), b = __ldcg(sv + i + T), c = __ldcg(sv + i + 2 * T),
-                        e = __ldcg(sv + i + 3 * T);
+            const uint4 a = load_src<kGlobal>(sv + i), b = load_src<kGlobal>(sv + i + T),
+                        c = load_src<kGlobal>(sv + i + 2 * T), e = load_src<kGlobal>(sv + i + 3 * T);
             dv[i] = a;
             dv[i + T] = b;
             dv[i + 2 * T] = c;
             dv[i + 3 * T] = e;
         }
 #pragma unroll 1
-        for (; i < nv; i += T) dv[i] = __ldcg(sv + i);
+        for (; i < nv; i += T) dv[i] = load_src<kGlobal>(sv + i);
 #pragma unroll 1
-        for (long long j = head + nv * kVec + t; j < n; j += T) dst[j] = __ldcg(src + j);
+        for (long long j = head + nv * kVec + t; j < n; j += T) dst[j] = load_src<kGlobal>(src + j);
         return;
     }
     long long i = t;
 #pragma unroll 1
     for (; i + 3 * T < n; i += 4 * T) {
-        const K a = __ldcg(src + i), b = __ldcg(src + i + T), c = __ldcg(src + i + 2 * T), e = __ldcg(src + i + 3 * T);
+        const K a = load_src<kGlobal>(src + i), b = load_src<kGlobal>(src + i + T), c = load_src<kGlobal>(src + i + 2 * T),
+                e = load_src<kGlobal>(src + i + 3 * T);
         dst[i] = a;
         dst[i + T] = b;
         dst[i + 2 * T] = c;
         dst[i + 3 * T] = e;
     }
 #pragma unroll 1
-    for (; i < n; i += T) dst[i] = __ldcg(src + i);
+    for (; i < n; i += T) dst[i] = load_src<kGlobal>(src + i);
+}
+
+// The source may be global or shared memory (a block's staging buffer).
+template <typename K>
+__device__ __forceinline__ void copy_keys(K* __restrict__ dst, const K* __restrict__ src, long long n, long long t,
+                                          long long T) {
+    if (__isShared(src)) copy_keys_from<false>(dst, src, n, t, T);
+    else copy_keys_from<true>(dst, src, n, t, T);
 }
 
 }  // namespace fifo_detail

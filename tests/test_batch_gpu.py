@@ -9,6 +9,7 @@ from oracle import pyoracle
 pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
+import gpuheap_gb300 as gh  # noqa: E402
 from gpuheap_gb300 import batch as gb  # noqa: E402
 
 
@@ -95,6 +96,60 @@ def test_knapsack_matches_dp():
         b.run("graph")
         res, _, _ = b.results()
         assert list(res) == want
+    finally:
+        b.close()
+
+
+def knapsack_set(ns):
+    w = np.array([50, 60, 70], np.int32)
+    inst = [("knapsack", (w, w + 5, 10)), ("knapsack", (w, w + 5, 1000)),
+            ("knapsack", (np.array([7], np.int32), np.array([9], np.int32), 7))]
+    return inst + [("knapsack", gb.gen_knapsack(n, 900 + n)) for n in ns]
+
+
+# instance sizes whose breadth-first frontier stays far below the 2^20-node
+# pool (a CPU breadth-first run of the same instances peaks below 40 K nodes)
+FIFO_SIZES = (2, 17, 100, 200, 300, 500)
+
+
+@pytest.mark.parametrize("order,counter", [("fifo", 20), ("switch", 20), ("switch", 2), ("heap", 20)])
+def test_knapsack_orders_match_oracle(order, counter):
+    """The knapsack models of the reference -- best-first on the heap,
+    breadth-first through the FIFO ring, and the heap/FIFO switch -- all
+    reach the CPU branch-and-bound optimum, mixed with A* instances."""
+    inst = small_mix(11)[:12] + knapsack_set(FIFO_SIZES)
+    want = oracle_results(inst)
+    b = gb.Batch(inst, batch_size=128, knapsack_order=order, switch_counter=counter)
+    try:
+        for mode in ("graph", "plain"):
+            b.run(mode)
+            res, st, stats = b.results()
+            assert not st.any(), st
+            assert np.array_equal(res, want), (order, mode, np.nonzero(res != want))
+        sw = b.knapsack_switches()
+        kinds = np.array([k == "knapsack" for k, _ in inst])
+        assert not sw[~kinds].any()
+        if order == "switch" and counter == 2:
+            assert sw[kinds].max() > 1, "expected heap/FIFO switches with a counter of 2"
+        if order in ("fifo", "heap"):
+            assert not sw.any()
+    finally:
+        b.close()
+
+
+def test_knapsack_fifo_overflow_is_reported():
+    """A breadth-first frontier wider than the node pool (800 items: over 3 M
+    nodes on the CPU) fails that instance with GH_ERR_CAPACITY; the other
+    instances of the batch still finish with their optimum."""
+    inst = knapsack_set((100, 800))
+    want = oracle_results(inst)
+    b = gb.Batch(inst, batch_size=128, knapsack_order="fifo")
+    try:
+        b.run("graph")
+        res, st, _ = b.results(check=False)
+        assert st[-1] == gh.GH_ERR_CAPACITY
+        assert not st[:-1].any()
+        assert np.array_equal(res[:-1], want[:-1])
     finally:
         b.close()
 
