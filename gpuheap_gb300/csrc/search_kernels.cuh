@@ -570,11 +570,20 @@ __device__ void run_sssp(const H& heap, Inst* in, unsigned char* smem, int heapO
     }
 }
 
+// Resident blocks per SM the build of the search kernel for blocks of up to
+// 256 threads is compiled for (512-thread blocks: one).  On the batched
+// workload (1024 grid A* + knapsack, batch 256) 3 measured 1011 ms per run,
+// 2 (128 registers) 1056 ms, 4 1109 ms and 1 (255 registers, few spills)
+// 1774 ms: resident blocks matter more than spills.
+constexpr int kSmallSearchBlocksPerSM = 3;
+
 // maxBatches > 0: each task takes at most that many batches, then the block
-// moves on (the search resumes in a later launch from its heap).
-template <typename H>
-__global__ void __launch_bounds__(kMaxSearchThreads, 1) k_search(H proto, Inst* insts, const int* tasks, int ntasks,
-                                                                 int* next, int maxBatches) {
+// moves on (the search resumes in a later launch from its heap).  MaxT is
+// the largest block it runs with; the register budget follows from it and
+// the blocks each SM should hold.
+template <typename H, int MaxT>
+__global__ void __launch_bounds__(MaxT, MaxT <= 256 ? kSmallSearchBlocksPerSM : 1)
+    k_search(H proto, Inst* insts, const int* tasks, int ntasks, int* next, int maxBatches) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_task;
     const int heapOff = static_cast<int>(SearchSmem::bytes(proto.batchSize, blockDim.x) / 4);
@@ -642,12 +651,19 @@ __global__ void k_search_collect(Inst* insts, const int* ids, int final, int bat
     }
 }
 
+// The search kernel built for `threads` threads per block.
+template <typename H>
+inline auto search_kernel(int threads) {
+    return threads <= 256 ? k_search<H, 256> : k_search<H, kMaxSearchThreads>;
+}
+
 template <typename H>
 cudaError_t launch_search(const H& proto, Inst* insts, const int* tasks, int ntasks, int* next, int grid, int threads,
                           size_t smem, cudaStream_t s, int maxBatches) {
-    cudaError_t e = cudaFuncSetAttribute(k_search<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    const auto kern = search_kernel<H>(threads);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    k_search<H><<<grid, threads, smem, s>>>(proto, insts, tasks, ntasks, next, maxBatches);
+    kern<<<grid, threads, smem, s>>>(proto, insts, tasks, ntasks, next, maxBatches);
     gh::impl::count_launch();
     return cudaGetLastError();
 }
@@ -690,8 +706,9 @@ inline int search_resident_blocks(const SearchConfig& c) {
     const size_t smem = search_smem(c);
     cudaError_t e = search_dispatch(c, [&](auto proto) {
         using H = decltype(proto);
-        cudaFuncSetAttribute(k_search<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_search<H>, T, smem);
+        const auto kern = search_kernel<H>(T);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, T, smem);
     });
     if (e != cudaSuccess || per < 1) per = 1;
     return per * c.numSMs;
