@@ -97,6 +97,22 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's time: the timed region ends when every rank's work
+    has; `dist` is None for one rank."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world_size, steps, ms):
+    """Whole-job rate in M units/s: every rank's units over the max-over-ranks time."""
+    return units_per_rank * world_size * steps / (ms / 1e3) / 1e6
+
+
 # ------------------------------------------------------------------ byte model
 def floor_log2_sum(M):
     """sum_{k=1..M} floor(log2 k)."""
@@ -333,10 +349,7 @@ def our_arm(args):
     t_reset = [e[0].elapsed_time(e[1]) for e in evs]
     t_ins = [e[1].elapsed_time(e[2]) for e in evs]
     t_del = [e[2].elapsed_time(e[3]) for e in evs]
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, "cuda")
 
     # correctness of the last step: the deleted stream is the input in key order
     if not torch.equal(out, want):
@@ -367,18 +380,15 @@ def our_arm(args):
         e1.record(stream)
         stream.synchronize()
         e2e_ms = e0.elapsed_time(e1)
-        if dist is not None:
-            t = torch.tensor([e2e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
+        e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
         if not torch.equal(host_out, want.cpu()):
             raise SystemExit("bench: e2e output is not the input in key order")
-        e2e = {"value": round(n * ws * args.steps / (e2e_ms / 1e3) / 1e6, 3), "unit": "M keys/s",
+        e2e = {"value": round(job_rate(n, ws, args.steps, e2e_ms), 3), "unit": "M keys/s",
                "h2d_bytes_per_step": n * s, "d2h_bytes_per_step": n * s,
                "ms_per_step": round(e2e_ms / args.steps, 3),
                "path": "pinned host keys -> cudaMemcpyAsync -> gh_heap_sort -> pinned host output"}
 
-    value = n * ws * args.steps / (total_ms / 1e3) / 1e6
+    value = job_rate(n, ws, args.steps, total_ms)
     ins_b, del_b = algorithmic_bytes(n, B, s, pb)
     ti, td = statistics.mean(t_ins), statistics.mean(t_del)
     kern, kb, kt = ("k_delete", del_b, td) if td >= ti else ("k_insert", ins_b, ti)
