@@ -55,7 +55,7 @@ def parse():
     p.add_argument("--cpu-sample-log2", type=int, default=27)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--timeout", type=float, default=2.0,
+    p.add_argument("--timeout", type=float, default=20.0,
                    help="device wait limit in seconds (raise it under a profiler)")
     p.add_argument("--workload", choices=["heapsort", "sssp", "batched", "served", "fifo"], default="heapsort",
                    help="heapsort: the plain heap-sort line (default); sssp: SSSP with the queue; "

@@ -107,7 +107,7 @@ extern "C" gh_status gh_sort_noalloc(int key_kind, int variant, int partial_buff
     d.initBits = key_kind == GH_KEY_U32 ? 0xffffffffull : key_kind == GH_KEY_I32 ? 0x7fffffffull : ~0ull;
     d.batchNum = batchNum;
     d.batchSize = batch_size;
-    d.timeoutNs = 2000000000LL;
+    d.timeoutNs = 20000000000LL;
     d.variant = variant;
     d.pb = partial_buffer ? 1 : 0;
     d.keyBytes = kb;
