@@ -112,27 +112,38 @@ def knapsack_set(ns):
 FIFO_SIZES = (2, 17, 100, 200, 300, 500)
 
 
-@pytest.mark.parametrize("order,counter", [("fifo", 20), ("switch", 20), ("switch", 2), ("heap", 20)])
+@pytest.mark.parametrize("order,counter", [("fifo", 20), ("switch", 20), ("switch", 2),
+                                           ("switch", 1), ("heap", 20)])
 def test_knapsack_orders_match_oracle(order, counter):
     """The knapsack models of the reference -- best-first on the heap,
     breadth-first through the FIFO ring, and the heap/FIFO switch -- all
-    reach the CPU branch-and-bound optimum, mixed with A* instances."""
+    reach the CPU branch-and-bound optimum, mixed with A* instances.
+
+    How many switches an instance makes depends on the block schedule (the
+    order children reach the queue and the pool slots they get), so only
+    their presence is checked: with a short counter at least one instance
+    leaves the heap, and with a counter of 1 one also comes back from the
+    FIFO ring, over the two runs."""
     inst = small_mix(11)[:12] + knapsack_set(FIFO_SIZES)
     want = oracle_results(inst)
+    kinds = np.array([k == "knapsack" for k, _ in inst])
     b = gb.Batch(inst, batch_size=128, knapsack_order=order, switch_counter=counter)
     try:
+        most = 0
         for mode in ("graph", "plain"):
             b.run(mode)
             res, st, stats = b.results()
             assert not st.any(), st
             assert np.array_equal(res, want), (order, mode, np.nonzero(res != want))
-        sw = b.knapsack_switches()
-        kinds = np.array([k == "knapsack" for k, _ in inst])
-        assert not sw[~kinds].any()
-        if order == "switch" and counter == 2:
-            assert sw[kinds].max() > 1, "expected heap/FIFO switches with a counter of 2"
-        if order in ("fifo", "heap"):
-            assert not sw.any()
+            sw = b.knapsack_switches()
+            assert not sw[~kinds].any()
+            if order in ("fifo", "heap"):
+                assert not sw.any()
+            most = max(most, int(sw[kinds].max()))
+        if order == "switch" and counter <= 2:
+            assert most >= 1, "expected a heap-to-FIFO switch with a short counter"
+        if order == "switch" and counter == 1:
+            assert most >= 2, "expected a FIFO-to-heap switch with a counter of 1"
     finally:
         b.close()
 
