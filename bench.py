@@ -33,7 +33,7 @@ import time
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
-METRIC = "M keys/s insert+delete, 2^28 u32"
+METRIC = "M keys/s insert+delete, 2^{log2n} {key}"
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -143,15 +143,19 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic(kernel, n, B, variant, pb):
-    """Per-launch DRAM bytes of `kernel` from profiles/traffic.json (an ncu
-    capture of a smaller case scaled by keys processed), or None."""
+def ncu_traffic(kernel, args, pb):
+    """DRAM bytes of one `kernel` launch as ncu measured them on this exact
+    workload (profiles/traffic.json), or None where no capture was taken.
+    Never scaled from another size: node traffic reaching DRAM grows faster
+    than the keys, as L2 holds a shrinking share of the upper levels."""
+    if args.grid or args.threads:
+        return None
     try:
         with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
             d = json.load(f)
-        e = d[f"{kernel}/{variant}/{'pb' if pb else 'np'}/B{B}"]
-        return e["dram_bytes_per_key"] * n
-    except Exception:
+        e = d[f"{kernel}/{args.variant}/{'pb' if pb else 'np'}/B{args.batch}/{args.key}/{args.dist}/2^{args.log2n}"]
+        return e["read"] + e["write"]
+    except (OSError, KeyError, ValueError):
         return None
 
 
@@ -249,9 +253,9 @@ def reference_arm(args):
     sample = (f"std::sort (per-thread std::sort + pairwise std::merge) of 2^{n_sample} u32 {args.dist} keys "
               f"per step on {threads} host threads; the reference has no CPU heap, its tests' CPU oracle is std::sort")
     line = {
-        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "M keys/s", "n_gpus": args.gpus,
+        "impl": "reference", "metric": METRIC.format(log2n=args.log2n, key="u32"), "value": round(value, 3), "unit": "M keys/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / len(times), 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.key, "data": "synthetic",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": workload_config(args),
         "cpu_baseline": {"value": round(value, 3), "unit": "M keys/s", "cores": threads, "kind": "port",
                          "sample": sample},
@@ -395,12 +399,13 @@ def our_arm(args):
     peak, peak_kind = peaks()
     achieved = kb / (kt / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 5), "traffic": ncu_traffic(kern, n, B, args.variant, pb),
+            "frac": round(achieved / peak, 5), "traffic": ncu_traffic(kern, args, pb),
             "kernel": kern, "peak_source": f"{peak_kind} hbm_gbs",
             "algorithmic_bytes": kb, "launch_ms": round(kt, 3),
-            "note": "achieved = closed-form BGPQ node bytes of the launch / its CUDA-event time; frac of measured"}
+            "note": "achieved = closed-form BGPQ node bytes of the launch / its CUDA-event time; frac of measured; "
+                    "traffic = ncu DRAM read+write bytes of one launch of this workload (1 pass), null if not captured"}
     line = {
-        "metric": METRIC, "value": round(value, 3), "unit": "M keys/s", "n_gpus": ws, "steps": args.steps,
+        "metric": METRIC.format(log2n=args.log2n, key=args.key), "value": round(value, 3), "unit": "M keys/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": args.key, "data": "synthetic",
         "config": dict(workload_config(args), block_threads=info["block_threads"], grid=info["grid"]),
