@@ -79,7 +79,6 @@ __global__ void __launch_bounds__(1024) k_sssp(H heap, const long long* __restri
     static_assert(sizeof(typename H::key_type) == 8, "SSSP keys are dist << 32 | vertex");
     extern __shared__ __align__(16) unsigned char smem[];
     const int B = heap.batchSize;
-    const int T = blockDim.x;
     const int tid = threadIdx.x;
     u64* batch = reinterpret_cast<u64*>(smem);
     u64* emit = batch + B;

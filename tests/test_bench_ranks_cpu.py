@@ -74,3 +74,26 @@ def test_reference_arm_line_on_one_rank():
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_roofline_traffic_is_the_capture_for_the_exact_workload():
+    """roofline.traffic is the ncu DRAM read+write of one launch of the
+    bench's own workload (profiles/traffic.json) and null for any other
+    size, layout or launch shape -- it is never scaled from another size."""
+    sys.path.insert(0, REPO)
+    import bench
+    sys_argv, sys.argv = sys.argv, ["bench.py"]
+    try:
+        a = bench.parse()
+    finally:
+        sys.argv = sys_argv
+    with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+        d = json.load(f)
+    e = d["k_delete/bottomup/pb/B2048/u32/uniform/2^28"]
+    assert bench.ncu_traffic("k_delete", a, True) == e["read"] + e["write"]
+    assert bench.ncu_traffic("k_insert", a, True) > 0
+    assert bench.ncu_traffic("k_delete", a, False) is None
+    a.log2n = 25
+    assert bench.ncu_traffic("k_delete", a, True) is None
+    a.log2n, a.grid = 28, 76
+    assert bench.ncu_traffic("k_delete", a, True) is None
