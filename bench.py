@@ -412,6 +412,7 @@ def our_arm(args):
         "phases_ms": {"reset": round(statistics.mean(t_reset), 3), "insert": round(ti, 3), "delete": round(td, 3)},
         "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
         "whole_sort_bytes_per_key": round((ins_b + del_b) / n, 2),
+        "io_lower_bound_bytes_per_key": 2 * s,
     }
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -420,6 +421,10 @@ def our_arm(args):
                                 "sample": f"std::sort of 2^{min(args.cpu_sample_log2, args.log2n)} u32 uniform keys "
                                           f"on {threads} threads (per-thread std::sort + pairwise std::merge), "
                                           f"median of 3"}
+        log2s = min(24, args.log2n)
+        v1, _ = cpu_sort_leg(log2s, args.seed, 1, reps=1)
+        line["cpu_single_thread"] = {"value": round(v1, 3), "unit": "M keys/s", "cores": 1,
+                                     "sample": f"std::sort of 2^{log2s} u32 uniform keys on one thread, once"}
     h.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
