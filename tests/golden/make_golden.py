@@ -9,8 +9,12 @@ phase and at the end.  These vectors pin both the oracle restatement (CPU
 tests) and the CUDA path (GPU tests, one thread block, where the heap is
 deterministic).
 
+Two sets: `small` (bgpq_ref_cases.npz, batch 16-64, every key type and
+scenario) and `large` (bgpq_ref_cases_large.npz, batch 256-2048, the batch
+sizes of the heap-sort configurations).
+
 Usage (needs the reference tree; not run by the tests):
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [small] [large]
 """
 import ctypes
 import json
@@ -96,72 +100,98 @@ def make_ops(rng, scenario, np_variant, B, n):
     return ops
 
 
-def main():
-    ref = ctypes.CDLL(LIB)
-    arrays = {}
-    meta = []
-    case = 0
+def run_case(ref, variant, kind, scenario, B, seed, rng, nb):
+    """Runs one seeded operation sequence through the reference's heap and
+    returns (arrays without the case prefix, meta)."""
+    np_variant = variant.endswith("_np")
+    n = nb * B
+    bn = 1
+    while bn * B < 2 * n:
+        bn <<= 1
+    dt, ct, lim = TYPES[kind]
+    keys = keys_for(rng, kind, n, scenario == "concurrent", ties=scenario == "ties")
+    ops = make_ops(rng, scenario, np_variant, B, n)
+    f = lambda name, res=ctypes.c_int: _fn(ref, variant, kind, name, res)
+    create = f("create", VP)
+    create.argtypes = [ctypes.c_int, ctypes.c_int, ct]
+    h = create(bn, B, lim)
+    out = np.zeros(n + 2 * B, dt)
+    dsizes = []
+    sz = ctypes.c_int()
+    pos = 0
+    snap_items = snap_counters = None
+    for op in ops:
+        if op > 0:
+            chunk = np.ascontiguousarray(keys[pos:pos + op])
+            pos += op
+            assert f("insert")(VP(h), VP(chunk.ctypes.data), op) == 0
+        elif op == 0:
+            assert f("delete")(VP(h), VP(out.ctypes.data), ctypes.byref(sz)) == 0
+            dsizes.append(sz.value)
+        else:
+            snap_items = np.zeros((bn + 1) * B, dt)
+            snap_counters = np.zeros(3, np.int32)
+            f("state")(VP(h), VP(snap_items.ctypes.data), None, VP(snap_counters.ctypes.data))
+            assert f("check")(VP(h)) == 1
+    items = np.zeros((bn + 1) * B, dt)
+    counters = np.zeros(3, np.int32)
+    f("state")(VP(h), VP(items.ctypes.data), None, VP(counters.ctypes.data))
+    f("destroy", None)(VP(h))
+    arrays = dict(keys=keys, ops=np.asarray(ops, np.int32), dsizes=np.asarray(dsizes, np.int32), out=out,
+                  snap_items=snap_items, snap_counters=snap_counters, items=items, counters=counters)
+    meta = dict(variant=variant, topdown=variant.startswith("td"), partial_buffer=not np_variant, key=kind,
+                batch_size=B, batch_num=bn, n=n, scenario=scenario, seed=seed)
+    return arrays, meta
+
+
+def small_cases():
+    """48 cases: 4 variants x {u32, u64, i32} x {sort, concurrent, mixed,
+    ties} at batch 16-64, 12-26 batches each."""
     for vi, variant in enumerate(VARIANTS):
         for ki, kind in enumerate(["u32", "u64", "i32"]):
             for si, scenario in enumerate(["sort", "concurrent", "mixed", "ties"]):
                 seed = 1000 + 97 * vi + 13 * ki + si
                 rng = np.random.default_rng(seed)
                 B = [16, 32, 64][(vi + ki + si) % 3]
-                np_variant = variant.endswith("_np")
                 # an even batch count keeps every insert of the _np variants
                 # full: a short insert there pads with init_limits keys that
                 # the bottom-up sift-down then chases past the allocation.
                 nb = 2 * int(rng.integers(6, 14))
-                n = nb * B
-                bn = 1
-                while bn * B < 2 * n:
-                    bn <<= 1
-                dt, ct, lim = TYPES[kind]
-                keys = keys_for(rng, kind, n, scenario == "concurrent", ties=scenario == "ties")
-                ops = make_ops(rng, scenario, np_variant, B, n)
-                f = lambda name, res=ctypes.c_int: _fn(ref, variant, kind, name, res)
-                create = f("create", VP)
-                create.argtypes = [ctypes.c_int, ctypes.c_int, ct]
-                h = create(bn, B, lim)
-                out = np.zeros(n + 2 * B, dt)
-                dsizes = []
-                sz = ctypes.c_int()
-                pos = 0
-                snap_items = snap_counters = None
-                for op in ops:
-                    if op > 0:
-                        chunk = np.ascontiguousarray(keys[pos:pos + op])
-                        pos += op
-                        assert f("insert")(VP(h), VP(chunk.ctypes.data), op) == 0
-                    elif op == 0:
-                        assert f("delete")(VP(h), VP(out.ctypes.data), ctypes.byref(sz)) == 0
-                        dsizes.append(sz.value)
-                    else:
-                        snap_items = np.zeros((bn + 1) * B, dt)
-                        snap_counters = np.zeros(3, np.int32)
-                        f("state")(VP(h), VP(snap_items.ctypes.data), None, VP(snap_counters.ctypes.data))
-                        assert f("check")(VP(h)) == 1
-                items = np.zeros((bn + 1) * B, dt)
-                counters = np.zeros(3, np.int32)
-                f("state")(VP(h), VP(items.ctypes.data), None, VP(counters.ctypes.data))
-                f("destroy", None)(VP(h))
-                p = f"c{case}_"
-                arrays[p + "keys"] = keys
-                arrays[p + "ops"] = np.asarray(ops, np.int32)
-                arrays[p + "dsizes"] = np.asarray(dsizes, np.int32)
-                arrays[p + "out"] = out
-                arrays[p + "snap_items"] = snap_items
-                arrays[p + "snap_counters"] = snap_counters
-                arrays[p + "items"] = items
-                arrays[p + "counters"] = counters
-                meta.append(dict(case=case, variant=variant, topdown=variant.startswith("td"),
-                                 partial_buffer=not np_variant, key=kind, batch_size=B,
-                                 batch_num=bn, n=n, scenario=scenario, seed=seed))
-                case += 1
-    arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)
-    path = os.path.join(HERE, "bgpq_ref_cases.npz")
-    np.savez_compressed(path, **arrays)
-    print(f"wrote {case} cases to {path} ({os.path.getsize(path)} bytes)")
+                yield variant, kind, scenario, B, seed, rng, nb
+
+
+def large_cases():
+    """16 cases at the batch sizes of the heap-sort configurations: per
+    variant a u32 sort at 2048, a u32 mixed run at 1024, a u64 two-phase
+    run at 256 and an i32 tie-heavy run at 512, 4-6 batches each (4 at
+    2048)."""
+    plan = [("u32", "sort", 2048), ("u32", "mixed", 1024), ("u64", "concurrent", 256), ("i32", "ties", 512)]
+    for vi, variant in enumerate(VARIANTS):
+        for pi, (kind, scenario, B) in enumerate(plan):
+            seed = 5000 + 97 * vi + 13 * pi
+            rng = np.random.default_rng(seed)
+            nb = 2 * int(rng.integers(2, 4))
+            if B == 2048:
+                nb = 4  # a three-level heap; keeps the fixture small
+            yield variant, kind, scenario, B, seed, rng, nb
+
+
+SETS = {"small": (small_cases, "bgpq_ref_cases.npz"), "large": (large_cases, "bgpq_ref_cases_large.npz")}
+
+
+def main(argv):
+    ref = ctypes.CDLL(LIB)
+    for name in (argv or ["small", "large"]):
+        gen, fname = SETS[name]
+        arrays, meta = {}, []
+        for case, params in enumerate(gen()):
+            a, m = run_case(ref, *params)
+            arrays.update({f"c{case}_{k}": v for k, v in a.items()})
+            meta.append(dict(case=case, **m))
+        arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)
+        path = os.path.join(HERE, fname)
+        np.savez_compressed(path, **arrays)
+        print(f"wrote {len(meta)} cases to {path} ({os.path.getsize(path)} bytes)")
 
 
 def _fn(lib, variant, kind, name, res):
@@ -171,4 +201,4 @@ def _fn(lib, variant, kind, name, res):
 
 
 if __name__ == "__main__":
-    sys.exit(main())
+    sys.exit(main(sys.argv[1:]))

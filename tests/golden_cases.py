@@ -1,28 +1,35 @@
-"""Loader for tests/golden/bgpq_ref_cases.npz (made by tests/golden/make_golden.py
-from the reference's own heap headers)."""
+"""Loader for the golden vectors made by tests/golden/make_golden.py from the
+reference's own heap headers: `small` (bgpq_ref_cases.npz, batch 16-64) and
+`large` (bgpq_ref_cases_large.npz, batch 256-2048)."""
 import json
 import os
 
 import numpy as np
 
-PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bgpq_ref_cases.npz")
-_data = None
+_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FILES = {"small": "bgpq_ref_cases.npz", "large": "bgpq_ref_cases_large.npz"}
+PATH = os.path.join(_DIR, FILES["small"])
+_data = {}
 
 
-def data():
-    global _data
-    if _data is None:
-        _data = np.load(PATH)
-    return _data
+def data(which="small"):
+    if which not in _data:
+        _data[which] = np.load(os.path.join(_DIR, FILES[which]))
+    return _data[which]
 
 
-def meta():
-    return json.loads(bytes(data()["meta"]).decode())
+def meta(which="small"):
+    return json.loads(bytes(data(which)["meta"]).decode())
 
 
-def case(i):
-    d = data()
+def case(i, which="small"):
+    d = data(which)
     p = f"c{i}_"
     out = {k[len(p):]: d[k] for k in d.files if k.startswith(p)}
-    out.update(meta()[i])
+    out.update(meta(which)[i])
     return out
+
+
+def all_ids():
+    """(set, index) of every golden case, for parametrising."""
+    return [(w, i) for w in FILES for i in range(len(meta(w)))]
