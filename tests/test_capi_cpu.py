@@ -62,3 +62,27 @@ def test_rejects_bad_arguments_before_touching_a_device(ghlib):
     assert ghlib.gh_serve_destroy(None) == 1
     assert ghlib.gh_serve_step(None, None, None, None, None) == 1
     assert ghlib.gh_serve_submit(None, 2, 0, 0, 0, None) == 1
+
+
+def test_newer_entry_points_reject_bad_arguments(ghlib):
+    """Delete below a threshold, GC, retrieval, single-block operations,
+    launch-shape setters and the knapsack order refuse a missing handle or
+    threshold with GH_ERR_INVALID, before any device work."""
+    t = ctypes.c_uint32(5)
+    n = ctypes.c_longlong()
+    sz = ctypes.c_int()
+    assert ghlib.gh_heap_delete_below(None, None, 0, ctypes.byref(t), ctypes.byref(n), None) == 1
+    assert ghlib.gh_heap_delete_below(None, None, 0, None, ctypes.byref(n), None) == 1      # no threshold
+    assert ghlib.gh_heap_gc(None, ctypes.byref(t), ctypes.byref(n), None) == 1
+    assert ghlib.gh_heap_retrieve(None, None, 0, ctypes.byref(sz), None) == 1
+    assert ghlib.gh_heap_insert_batch(None, None, 1, None) == 1
+    assert ghlib.gh_heap_delete_batch(None, None, ctypes.byref(sz), None) == 1
+    assert ghlib.gh_heap_set_timeout(None, 1.0) == 1
+    assert ghlib.gh_heap_set_block_threads(None, 0) == 1
+    assert ghlib.gh_heap_set_grid(None, 0) == 1
+    assert ghlib.gh_heap_inject_lock(None, 0, 1) == 1
+    assert ghlib.gh_batch_set_knapsack_order(None, 0, 20) == 1
+    assert ghlib.gh_batch_knapsack_switches(None, None, None) == 1
+    assert ghlib.gh_batch_set_astar_blocks(None, 1 << 18, 8) == 1
+    assert ghlib.gh_batch_set_timeout(None, 1.0) == 1
+    assert ghlib.gh_serve_set_blocks(None, 1 << 15, 24, 1 << 18, 8) == 1
