@@ -1,0 +1,283 @@
+"""Explicit-state models of the heap's lock protocols, explored over every
+interleaving of their atomic steps.  Test infrastructure only: nothing in
+the library imports it.
+
+The device code keeps one status word per node and moves it with CAS,
+atomicMax and release stores (include/gpuheap_device.cuh).  Two hand-offs
+between blocks are easy to get wrong and cannot be tested exhaustively on
+a GPU, so they are modelled here at the level of those atomic steps:
+
+* bottom-up parks (gpuheap_device.cuh `insert_bottomup`, `tryChild`,
+  `refill_and_sift`; reference heap/buitdd/heap.cuh:372-418, 636-683):
+  an insert that cannot lock its parent parks its node so that deleters
+  can pass through it or take it as the last node, then takes it back with
+  atomicMax.  Finding its own park value there must prove that nobody held
+  the node meanwhile, or the insert would keep a stale copy of the batch.
+* the top-down hand-off (`insert_topdown`, `takeLastTopDown`; reference
+  heap/tditdd/heap.cuh:371-393, 683-744): a deleter whose last node is an
+  insert's target still in flight marks it, and the insert hands its batch
+  over at the root instead of writing the target.  The batch must reach
+  the deleter exactly once, and neither side may wait forever.
+
+A spin wait is a step that is enabled only when its condition holds, so a
+state where no actor can move but some have not finished is a deadlock.
+Each model takes switches that plant the mistakes the protocol exists to
+prevent; the tests check that the explorer finds them.
+"""
+from collections import namedtuple
+from dataclasses import dataclass, field
+
+# status word values (gpuheap_device.cuh: struct BU, struct TD)
+AVAIL, INSHOLD, DELMOD, INUSE = 0, 1, 2, 1 << 30
+TD_AVAIL, TD_INUSE, TD_TARGET, TD_MARKED = 0, 1, 2, 3
+PARK_BASE = 4  # tickets: PARK_BASE.. (below INUSE)
+
+
+class Violation(AssertionError):
+    """An invariant broke; `trace` is the interleaving that broke it."""
+
+    def __init__(self, msg, trace):
+        super().__init__(f"{msg}; trace: {' -> '.join(trace)}")
+        self.trace = trace
+
+
+@dataclass
+class Result:
+    states: int = 0
+    finals: int = 0
+    deadlocks: list = field(default_factory=list)
+
+
+def explore(initial, actors, check_final=None, limit=2_000_000):
+    """Depth-first search over every interleaving.  `initial` is a tuple
+    (global state, one program counter per actor); each actor is a function
+    (state, pc) -> list of (label, new_state, new_pc), empty when it is
+    blocked or done (pc None).  `check_final(state)` runs at every state
+    where all actors are done.  Raises Violation from an actor step or the
+    final check; returns the number of states and any deadlocks (with the
+    trace that reached them)."""
+    res = Result()
+    seen = set()
+    stack = [(initial, ())]
+    while stack:
+        (g, pcs), trace = stack.pop()
+        key = (g, pcs)
+        if key in seen:
+            continue
+        seen.add(key)
+        res.states += 1
+        if res.states > limit:
+            raise RuntimeError("state space larger than the limit")
+        moves = []
+        for i, act in enumerate(actors):
+            if pcs[i] is None:
+                continue
+            for label, g2, pc2 in act(g, pcs[i], trace):
+                moves.append((i, label, g2, pc2))
+        if not moves:
+            if all(pc is None for pc in pcs):
+                res.finals += 1
+                if check_final:
+                    check_final(g, list(trace))
+            else:
+                res.deadlocks.append(list(trace))
+            continue
+        for i, label, g2, pc2 in moves:
+            pcs2 = pcs[:i] + (pc2,) + pcs[i + 1:]
+            stack.append(((g2, pcs2), trace + (f"{actors[i].__name__}:{label}",)))
+    return res
+
+
+def _set(g, **kw):
+    d = g._asdict()
+    d.update(kw)
+    return type(g)(**d)
+
+
+# --------------------------------------------------------------------------
+# bottom-up parks
+
+BUState = namedtuple("BUState", "x p ver seen_i seen_i2 t_done in_heap")
+
+
+def bottomup_park_model(tagged=True, trust_own_park=True, delmod_on_release=True, with_taker=True,
+                        with_passer=True):
+    """Node x with parent p.  Actors:
+
+    * `ins` holds x (INUSE) with its batch cached; p is held by `holder`, so
+      its first attempt at p fails and it parks x, locks p, takes x back
+      with atomicMax and trusts its cache only if it finds its own park
+      value (`insert_bottomup`).
+    * `holder` holds p and either releases it, or first passes through x as
+      a sifting deleter: atomicMax on x, write x, release x as DELMOD if it
+      found a park value (`tryChild`), else as it found it.
+    * `taker` takes x as the last node (atomicMax, reset, release AVAIL;
+      `refill_and_sift`), after which `ins2` claims x as its new target,
+      writes its batch, fails on p and parks x with its own value.
+
+    ver counts writes of x; an insert that trusts its cache asserts that
+    ver is what it was at its park.  tagged=False parks every insert with
+    the one value INSHOLD (the reference's protocol, which then must never
+    trust); delmod_on_release=False restores the raw park value after a
+    pass-through."""
+    tag_i = PARK_BASE if tagged else INSHOLD
+    tag_i2 = PARK_BASE + 1 if tagged else INSHOLD
+
+    def parked(v):
+        return v == INSHOLD or PARK_BASE <= v < INUSE
+
+    def ins(g, pc, trace):
+        if pc == "try_p":  # one attempt at the parent first
+            if g.p == AVAIL:
+                return [("cas p ok", _set(g, p=INUSE), "own_p")]
+            return [("cas p fail; park x", _set(g, x=tag_i, seen_i=g.ver), "lock_p")]
+        if pc == "lock_p":
+            return [("lock p", _set(g, p=INUSE), "retake")] if g.p == AVAIL else []
+        if pc == "retake":  # atomicMax(x, INUSE), spinning while INUSE
+            if g.x == INUSE:
+                return []
+            trust = trust_own_park and g.x == tag_i
+            if trust and g.ver != g.seen_i:
+                raise Violation("insert trusted a stale copy of its parked node", list(trace) + ["ins:retake"])
+            return [(f"retake x (found {g.x}, {'trust' if trust else 'reload'})", _set(g, x=INUSE), "own_p")]
+        if pc == "own_p":  # write x and p, release both
+            return [("write, release x and p", _set(g, x=AVAIL, p=AVAIL, ver=g.ver + 1), None)]
+        return []
+
+    def holder(g, pc, trace):
+        if pc == "hold":
+            moves = [("release p", _set(g, p=AVAIL), None)]
+            if with_passer:
+                moves.append(("sift toward x", g, "take_x"))
+            return moves
+        if pc == "take_x":
+            if not g.in_heap:  # taken as the last node and not claimed again: the sift finds no child
+                return [("x absent, release p", _set(g, p=AVAIL), None)]
+            if g.x == INUSE:
+                return []
+            back = DELMOD if (delmod_on_release and parked(g.x)) else g.x
+            return [(f"take x (found {g.x})", _set(g, x=INUSE), ("wrote", back))]
+        if isinstance(pc, tuple) and pc[0] == "wrote":
+            return [(f"write x, release x as {pc[1]}, release p", _set(g, x=pc[1], ver=g.ver + 1, p=AVAIL), None)]
+        return []
+
+    def taker(g, pc, trace):
+        if pc == "take":
+            if g.x == INUSE:
+                return []
+            return [(f"take last x (found {g.x})", _set(g, x=INUSE), "reset")]
+        if pc == "reset":
+            return [("reset x, release AVAIL", _set(g, x=AVAIL, ver=g.ver + 1, t_done=True, in_heap=False), None)]
+        return []
+
+    def ins2(g, pc, trace):
+        if pc == "claim":  # x is the next target only after the taker lowered the count
+            if not g.t_done or g.x != AVAIL:
+                return []
+            return [("claim x", _set(g, x=INUSE, in_heap=True), "write")]
+        if pc == "write":
+            return [("write x", _set(g, ver=g.ver + 1), "try_p")]
+        if pc == "try_p":
+            if g.p == AVAIL:
+                return [("cas p ok", _set(g, p=INUSE), "own_p")]
+            return [("cas p fail; park x", _set(g, x=tag_i2, seen_i2=g.ver), "lock_p")]
+        if pc == "lock_p":
+            return [("lock p", _set(g, p=INUSE), "retake")] if g.p == AVAIL else []
+        if pc == "retake":
+            if g.x == INUSE:
+                return []
+            trust = trust_own_park and g.x == tag_i2
+            if trust and g.ver != g.seen_i2:
+                raise Violation("insert trusted a stale copy of its parked node", list(trace) + ["ins2:retake"])
+            return [(f"retake x (found {g.x})", _set(g, x=INUSE), "own_p")]
+        if pc == "own_p":
+            return [("write, release x and p", _set(g, x=AVAIL, p=AVAIL, ver=g.ver + 1), None)]
+        return []
+
+    actors = [ins, holder]
+    pcs = ["try_p", "hold"]
+    if with_taker:
+        actors += [taker, ins2]
+        pcs += ["take", "claim"]
+    g0 = BUState(x=INUSE, p=INUSE, ver=0, seen_i=-1, seen_i2=-1, t_done=not with_taker, in_heap=True)
+
+    def final(g, trace):
+        if g.x != AVAIL or g.p != AVAIL:
+            raise Violation(f"a lock word left taken (x={g.x}, p={g.p})", trace)
+
+    return (g0, tuple(pcs)), actors, final
+
+
+# --------------------------------------------------------------------------
+# top-down hand-off
+
+TDState = namedtuple("TDState", "t root t_batch got steps")
+
+
+def topdown_handoff_model(path_steps=2, check_marked_on_path=True, cas_at_target=True, wait_for_handoff=True):
+    """One insert on its way down to target t (`path_steps` path nodes still
+    ahead) and one deleter that holds the root and wants t as its last node.
+
+    * `ins` checks at every path step whether t was MARKED and then hands
+      its batch over at the root; at the end it takes t with
+      CAS(TARGET -> INUSE): found MARKED, it hands over; else it writes its
+      batch to t and releases it (`insert_topdown`).  A hand-over writes
+      the root and turns MARKED back into TARGET.
+    * `dele` takes t with CAS(AVAIL -> INUSE), or marks it with
+      CAS(TARGET -> MARKED) and then waits for CAS(TARGET -> AVAIL) before
+      it reads the root (`takeLastTopDown`).
+
+    got counts the deleter's receipts of the insert's batch: it must be 1
+    at the end, from t or from the root, never both.  Planted mistakes:
+    the insert ignores MARKED on its path, writes t with a plain store, or
+    the deleter reads the root without waiting for the hand-off."""
+
+    def ins(g, pc, trace):
+        if isinstance(pc, int):  # pc = path steps still ahead; each reads t first
+            if check_marked_on_path and g.t == TD_MARKED:
+                return [("sees MARKED on the path", g, "handover")]
+            return [(f"path step ({pc} left)", g, pc - 1 if pc > 0 else "at_target")]
+        if pc == "at_target":  # a separate step: the deleter may mark t in between
+            if cas_at_target:
+                if g.t == TD_TARGET:
+                    return [("cas t TARGET->INUSE", _set(g, t=TD_INUSE), "write_t")]
+                return [(f"cas t fails (found {g.t}): hand over", g, "handover")]
+            return [("store t INUSE (no cas)", _set(g, t=TD_INUSE), "write_t")]
+        if pc == "write_t":
+            return [("write t, release AVAIL", _set(g, t_batch=True, t=TD_AVAIL), None)]
+        if pc == "handover":
+            return [("write root", _set(g, root=True), "signal")]
+        if pc == "signal":
+            return [("t MARKED->TARGET", _set(g, t=TD_TARGET), None)]
+        return []
+
+    def dele(g, pc, trace):
+        if pc == "take":
+            moves = []
+            if g.t == TD_AVAIL:
+                moves.append(("cas t AVAIL->INUSE", _set(g, t=TD_INUSE), "read_t"))
+            if g.t == TD_TARGET:
+                moves.append(("cas t TARGET->MARKED", _set(g, t=TD_MARKED), "wait"))
+            return moves
+        if pc == "read_t":
+            if not g.t_batch:
+                raise Violation("deleter took t before the insert wrote it", list(trace) + ["dele:read_t"])
+            return [("read t, reset, release", _set(g, got=g.got + 1, t_batch=False, t=TD_AVAIL), None)]
+        if pc == "wait":
+            if not wait_for_handoff:
+                return [("read root without waiting", g, "read_root")]
+            return [("cas t TARGET->AVAIL", _set(g, t=TD_AVAIL), "read_root")] if g.t == TD_TARGET else []
+        if pc == "read_root":
+            if not g.root:
+                raise Violation("deleter read the root before the hand-over", list(trace) + ["dele:read_root"])
+            return [("read root", _set(g, got=g.got + 1, root=False), None)]
+        return []
+
+    def final(g, trace):
+        if g.got != 1 or g.root or g.t_batch:
+            raise Violation(f"batch received {g.got} times (root {g.root}, t {g.t_batch})", trace)
+        if g.t != TD_AVAIL:
+            raise Violation(f"t left in state {g.t}", trace)
+
+    g0 = TDState(t=TD_TARGET, root=False, t_batch=False, got=0, steps=path_steps)
+    return (g0, (path_steps, "take")), [ins, dele], final

@@ -1,0 +1,95 @@
+"""Race detection for the heap's lock hand-offs, on CPU: every interleaving
+of the atomic steps of the bottom-up park protocol and of the top-down
+target hand-off (oracle/lock_model.py) keeps its invariants and never
+deadlocks, and the explorer finds each planted mistake -- the ones these
+protocols exist to prevent -- with the interleaving that exposes it."""
+import pytest
+
+from oracle import lock_model as lm
+
+
+def _run(model):
+    init, actors, final = model
+    return lm.explore(init, actors, final)
+
+
+@pytest.mark.parametrize("with_taker", [True, False])
+@pytest.mark.parametrize("with_passer", [True, False])
+def test_ticketed_parks_are_safe(with_taker, with_passer):
+    """The device protocol: tickets unique per insert, trust on finding
+    one's own ticket, DELMOD after a pass-through."""
+    r = _run(lm.bottomup_park_model(with_taker=with_taker, with_passer=with_passer))
+    assert r.finals >= 1 and not r.deadlocks
+
+
+def test_reference_parks_are_safe_without_trust():
+    """The reference's protocol: one INSHOLD value, and the node is always
+    read back from memory (heap/buitdd/heap.cuh:643-673)."""
+    r = _run(lm.bottomup_park_model(tagged=False, trust_own_park=False))
+    assert r.finals >= 1 and not r.deadlocks
+
+
+def test_untagged_parks_with_trust_are_caught():
+    """Trusting INSHOLD without tickets loses a batch: a deleter takes the
+    parked node as its last node, a new insert claims it and parks there
+    too, and the first insert finds 'its' park value again."""
+    with pytest.raises(lm.Violation) as e:
+        _run(lm.bottomup_park_model(tagged=False, with_passer=False))
+    trace = e.value.trace
+    assert any(t.startswith("taker:take last x") for t in trace)
+    assert any(t.startswith("ins2:cas p fail; park x") for t in trace)
+    assert trace[-1].endswith("retake")
+
+
+def test_restoring_the_ticket_after_a_pass_through_is_caught():
+    """A deleter that passed through a parked node must leave DELMOD, not
+    the ticket it found (gpuheap_device.cuh tryChild)."""
+    with pytest.raises(lm.Violation) as e:
+        _run(lm.bottomup_park_model(delmod_on_release=False))
+    assert any("release x as" in t and "as 2" not in t for t in e.value.trace)
+
+
+@pytest.mark.parametrize("steps", [0, 1, 2, 4])
+@pytest.mark.parametrize("check_on_path", [True, False])
+def test_topdown_handoff_is_safe(steps, check_on_path):
+    """The batch reaches the deleter exactly once and t ends AVAIL, whether
+    the insert sees the mark on its path or at its final CAS -- the path
+    check only shortens the deleter's wait."""
+    r = _run(lm.topdown_handoff_model(path_steps=steps, check_marked_on_path=check_on_path))
+    assert r.finals == 1 and not r.deadlocks
+
+
+def test_topdown_plain_store_at_the_target_deadlocks():
+    """Writing t with a plain store ignores a mark set after the last path
+    check: the deleter then waits forever for the hand-over."""
+    r = _run(lm.topdown_handoff_model(cas_at_target=False))
+    assert r.deadlocks
+    dl = r.deadlocks[0]
+    assert "dele:cas t TARGET->MARKED" in dl and "ins:store t INUSE (no cas)" in dl
+
+
+def test_topdown_reading_the_root_before_the_handoff_is_caught():
+    with pytest.raises(lm.Violation, match="before the hand-over"):
+        _run(lm.topdown_handoff_model(wait_for_handoff=False))
+
+
+def test_explorer_reports_deadlock_and_final_states():
+    """The explorer itself: two actors that each wait for the other's flag
+    deadlock; one that sets a flag first lets the other finish."""
+    from collections import namedtuple
+    S = namedtuple("S", "a b")
+
+    def first(g, pc, trace):
+        if pc == 0:
+            return [("wait b", g, 1)] if g.b else []
+        return [("set a", S(True, g.b), None)] if pc == 1 else []
+
+    def second(g, pc, trace):
+        if pc == 0:
+            return [("wait a", g, 1)] if g.a else []
+        return [("set b", S(g.a, True), None)] if pc == 1 else []
+
+    r = lm.explore((S(False, False), (0, 0)), [first, second])
+    assert r.deadlocks == [[]] and r.finals == 0
+    r = lm.explore((S(False, True), (0, 0)), [first, second])
+    assert not r.deadlocks and r.finals == 1
