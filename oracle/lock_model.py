@@ -4,8 +4,8 @@ the library imports it.
 
 The device code keeps one status word per node and moves it with CAS,
 atomicMax and release stores (include/gpuheap_device.cuh).  Two hand-offs
-between blocks are easy to get wrong and cannot be tested exhaustively on
-a GPU, so they are modelled here at the level of those atomic steps:
+between blocks, and the search's termination, are easy to get wrong and
+cannot be tested exhaustively on a GPU, so they are modelled here at the level of those atomic steps:
 
 * bottom-up parks (gpuheap_device.cuh `insert_bottomup`, `tryChild`,
   `refill_and_sift`; reference heap/buitdd/heap.cuh:372-418, 636-683):
@@ -18,6 +18,9 @@ a GPU, so they are modelled here at the level of those atomic steps:
   insert's target still in flight marks it, and the insert hands its batch
   over at the root instead of writing the target.  The batch must reach
   the deleter exactly once, and neither side may wait forever.
+* termination of a search (gpuheap_gb300/csrc/worklist.cuh): blocks that
+  share one heap count themselves busy while they hold work; the search
+  must end exactly when the work is done, with no block left waiting.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -281,3 +284,78 @@ def topdown_handoff_model(path_steps=2, check_marked_on_path=True, cas_at_target
 
     g0 = TDState(t=TD_TARGET, root=False, t_batch=False, got=0, steps=path_steps)
     return (g0, (path_steps, "take")), [ins, dele], final
+
+
+# --------------------------------------------------------------------------
+# termination of a search whose blocks share one heap
+
+TermState = namedtuple("TermState", "heap busy processed")
+
+
+def termination_model(blocks=2, depth=2, count_while_waiting=False):
+    """The busy-counter protocol of gpuheap_gb300/csrc/worklist.cuh
+    (`wait_for_keys`, `batch_done`; the reference stops on a count of
+    active blocks, applications/sssp_longfei_new/sssp.cu:19-132).
+
+    Work is a binary tree: taking a unit of depth d > 0 inserts two units
+    of depth d - 1, one insert at a time; the heap starts with one unit of
+    depth `depth`.  Each block loops: wait -> count itself busy -> take a
+    unit (or find none) -> insert its children -> uncount -> wait.  A waiting
+    block leaves when it reads busy == 0 and then, in a separate step, finds
+    the heap empty.  Invariant at the end: every unit was taken, the heap is
+    empty and busy is 0; no state may leave blocks waiting on each other.
+
+    count_while_waiting=True plants the mistake the protocol avoids: a
+    waiting block counts itself busy, so waiting blocks keep each other
+    alive and the search never ends."""
+    total = 2 ** (depth + 1) - 1
+
+    def block(g, pc, trace):
+        if pc == "wait":
+            if count_while_waiting:
+                return [("count self while waiting", _set(g, busy=g.busy + 1), "wait_counted")]
+            moves = []
+            if g.heap:
+                moves.append(("sees keys", g, "count"))
+            if g.busy == 0:
+                moves.append(("reads busy 0", g, "recheck"))
+            return moves  # heap empty and others busy: spin
+        if pc == "wait_counted":
+            moves = []
+            if g.heap:
+                moves.append(("sees keys", g, "take"))
+            if g.busy == 0:
+                moves.append(("reads busy 0", g, None))
+            return moves
+        if pc == "recheck":
+            if not g.heap:
+                return [("heap empty: leave", g, None)]
+            return [("keys again", g, "wait")]
+        if pc == "count":
+            return [("busy += 1", _set(g, busy=g.busy + 1), "take")]
+        if pc == "take":
+            if not g.heap:
+                return [("empty deleteRoot", g, "done")]
+            d = g.heap[0]
+            return [(f"take unit {d}", _set(g, heap=g.heap[1:], processed=g.processed + 1), ("ins", d - 1, 2 if d > 0 else 0))]
+        if isinstance(pc, tuple) and pc[0] == "ins":
+            _, d, left = pc
+            if left == 0:
+                return [("inserts done", g, "done")]
+            return [(f"insert unit {d}", _set(g, heap=tuple(sorted(g.heap + (d,), reverse=True))), ("ins", d, left - 1))]
+        if pc == "done":
+            return [("busy -= 1", _set(g, busy=g.busy - 1), "wait")]
+        return []
+
+    actors = []
+    for i in range(blocks):
+        def b(g, pc, trace, _f=block):
+            return _f(g, pc, trace)
+        b.__name__ = f"block{i}"
+        actors.append(b)
+
+    def final(g, trace):
+        if g.heap or g.busy != 0 or g.processed != total:
+            raise Violation(f"search ended with heap {g.heap}, busy {g.busy}, {g.processed}/{total} units", trace)
+
+    return (TermState(heap=(depth,), busy=0, processed=0), tuple(["wait"] * blocks)), actors, final

@@ -1,7 +1,7 @@
 """Race detection for the heap's lock hand-offs, on CPU: every interleaving
-of the atomic steps of the bottom-up park protocol and of the top-down
-target hand-off (oracle/lock_model.py) keeps its invariants and never
-deadlocks, and the explorer finds each planted mistake -- the ones these
+of the atomic steps of the bottom-up park protocol, of the top-down target
+hand-off and of the searches' termination protocol (oracle/lock_model.py)
+keeps its invariants and never deadlocks, and the explorer finds each planted mistake -- the ones these
 protocols exist to prevent -- with the interleaving that exposes it."""
 import pytest
 
@@ -93,3 +93,19 @@ def test_explorer_reports_deadlock_and_final_states():
     assert r.deadlocks == [[]] and r.finals == 0
     r = lm.explore((S(False, True), (0, 0)), [first, second])
     assert not r.deadlocks and r.finals == 1
+
+
+@pytest.mark.parametrize("blocks,depth", [(2, 2), (3, 2), (2, 3)])
+def test_termination_protocol_ends_exactly_when_work_is_done(blocks, depth):
+    """worklist.cuh: in every interleaving each block leaves, and only once
+    every unit of the work tree was taken, the heap is empty and busy is 0."""
+    r = _run(lm.termination_model(blocks=blocks, depth=depth))
+    assert r.finals == 1 and not r.deadlocks
+
+
+def test_waiting_blocks_counted_busy_never_end():
+    """Planted: a waiting block that counts itself busy keeps the others
+    waiting forever once the work runs out."""
+    r = _run(lm.termination_model(count_while_waiting=True))
+    assert r.deadlocks and r.finals == 0
+    assert all("count self while waiting" in t for t in r.deadlocks[0][-2:])
