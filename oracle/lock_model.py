@@ -5,7 +5,8 @@ the library imports it.
 The device code keeps one status word per node and moves it with CAS,
 atomicMax and release stores (include/gpuheap_device.cuh).  Two hand-offs
 between blocks, and the search's termination, are easy to get wrong and
-cannot be tested exhaustively on a GPU, so they are modelled here at the level of those atomic steps:
+cannot be tested exhaustively on a GPU, so they are modelled here at the
+level of those atomic steps:
 
 * bottom-up parks (gpuheap_device.cuh `insert_bottomup`, `tryChild`,
   `refill_and_sift`; reference heap/buitdd/heap.cuh:372-418, 636-683):
