@@ -1,12 +1,12 @@
-"""Explicit-state models of the heap's lock protocols, explored over every
-interleaving of their atomic steps.  Test infrastructure only: nothing in
-the library imports it.
+"""Explicit-state models of the path's lock-free protocols, explored over
+every interleaving of their atomic steps.  Test infrastructure only: nothing
+in the library imports it.
 
-The device code keeps one status word per node and moves it with CAS,
-atomicMax and release stores (include/gpuheap_device.cuh).  Two hand-offs
-between blocks, and the search's termination, are easy to get wrong and
-cannot be tested exhaustively on a GPU, so they are modelled here at the
-level of those atomic steps:
+The device code moves its shared words with CAS, atomicMax, atomicAdd and
+release stores (include/gpuheap_device.cuh, include/gpuheap_fifo.cuh).  The
+hand-offs between blocks, the FIFO ring and the search's termination are
+easy to get wrong and cannot be tested exhaustively on a GPU, so they are
+modelled here at the level of those atomic steps:
 
 * bottom-up parks (gpuheap_device.cuh `insert_bottomup`, `tryChild`,
   `refill_and_sift`; reference heap/buitdd/heap.cuh:372-418, 636-683):
@@ -19,6 +19,9 @@ level of those atomic steps:
   insert's target still in flight marks it, and the insert hands its batch
   over at the root instead of writing the target.  The batch must reach
   the deleter exactly once, and neither side may wait forever.
+* the FIFO buffer (include/gpuheap_fifo.cuh): pushes publish and pops
+  free in reservation and claim order on a ring that wraps, so no key is
+  read before it is written or overwritten before it is read.
 * termination of a search (gpuheap_gb300/csrc/worklist.cuh): blocks that
   share one heap count themselves busy while they hold work; the search
   must end exactly when the work is done, with no block left waiting.
@@ -360,3 +363,112 @@ def termination_model(blocks=2, depth=2, count_while_waiting=False):
             raise Violation(f"search ended with heap {g.heap}, busy {g.busy}, {g.processed}/{total} units", trace)
 
     return (TermState(heap=(depth,), busy=0, processed=0), tuple(["wait"] * blocks)), actors, final
+
+
+# --------------------------------------------------------------------------
+# the FIFO buffer
+
+FifoState = namedtuple("FifoState", "slots end write read begin out")
+
+
+def fifo_model(pushes=(1, 1, 1), pops=(1, 1, 1), capacity=2, wait_room=True, publish_in_order=True,
+               claim_by_cas=True, free_in_order=True):
+    """gh::Fifo<K> (include/gpuheap_fifo.cuh `push`, `claim`, `copy_out`,
+    `release`; reference artifacts/buffer/buffer.cuh:127-213) on a ring of
+    `capacity` slots.  Pusher i reserves pushes[i] positions with
+    atomicAdd(end), waits until its last slot is within one lap of begin,
+    writes its slots one at a time, waits until write reaches its start and
+    stores its end.  Popper j takes pops[j] keys in as many pops as it
+    needs: it waits until something is published, reads read and write in
+    two steps, claims what is there (up to what it still needs) with a CAS
+    on read, retrying when it lost, copies its slots one at a time, waits
+    until begin reaches its start and stores its end.
+
+    A slot holds (position, key).  Invariants: every copy finds the key
+    pushed for that position (each claim is a run of consecutive positions,
+    so a popper receives keys in push order), and at the end every key came
+    out exactly once and the four positions agree.  Planted mistakes: no room wait, publishing
+    without waiting for earlier pushes, claiming with a plain store, and
+    freeing without waiting for earlier pops."""
+    assert sum(pushes) == sum(pops)
+    total = sum(pushes)
+
+    def pusher(i):
+        size = pushes[i]
+
+        def push(g, pc, trace):
+            if pc == "reserve":
+                return [(f"reserve [{g.end},{g.end + size})", _set(g, end=g.end + size), ("room", g.end))]
+            kind, start = pc[0], pc[1]
+            if kind == "room":
+                if wait_room and start + size - g.begin > capacity:
+                    return []
+                return [("room", g, ("put", start, 0))]
+            if kind == "put":
+                k = pc[2]
+                if k == size:
+                    return [("written", g, ("publish", start))]
+                pos = start + k
+                slots = list(g.slots)
+                slots[pos % capacity] = (pos, pos)  # the key pushed for position pos is pos
+                return [(f"write slot {pos % capacity} <- {pos}", _set(g, slots=tuple(slots)), ("put", start, k + 1))]
+            if kind == "publish":
+                if publish_in_order and g.write != start:
+                    return []
+                return [(f"write = {start + size}", _set(g, write=max(g.write, start + size) if not publish_in_order
+                                                         else start + size), None)]
+            return []
+        push.__name__ = f"push{i}"
+        return push
+
+    def popper(j):
+        def pop(g, pc, trace):
+            # pc[-1] = keys this popper still has to take; it pops until then
+            if pc[0] == "wait":
+                return [("sees keys", g, ("r", pc[1]))] if g.write > g.read else []
+            if pc[0] == "r":
+                return [(f"reads read={g.read}", g, ("w", g.read, pc[1]))]
+            if pc[0] == "w":
+                _, r, left = pc
+                n = min(max(g.write - r, 0), left)
+                if n == 0:
+                    return [("nothing left at r: retry", g, ("wait", left))]
+                return [(f"reads write={g.write}", g, ("cas", r, n, left))]
+            if pc[0] == "cas":
+                _, r, n, left = pc
+                if claim_by_cas and g.read != r:
+                    return [("cas lost", g, ("wait", left))]
+                return [(f"claims [{r},{r + n})", _set(g, read=r + n if claim_by_cas else max(g.read, r + n)),
+                         ("copy", r, n, 0, left))]
+            if pc[0] == "copy":
+                _, start, n, k, left = pc
+                if k == n:
+                    return [("copied", g, ("free", start, n, left))]
+                pos = start + k
+                slot = g.slots[pos % capacity]
+                if slot != (pos, pos):
+                    raise Violation(f"popper read slot {pos % capacity} for position {pos} and found {slot}",
+                                    list(trace) + [f"pop{j}:copy {pos}"])
+                return [(f"copies {pos}", _set(g, out=g.out + (pos,)), ("copy", start, n, k + 1, left))]
+            if pc[0] == "free":
+                _, start, n, left = pc
+                if free_in_order and g.begin != start:
+                    return []
+                nxt = ("wait", left - n) if left > n else None
+                return [(f"begin = {start + n}", _set(g, begin=start + n if free_in_order else max(g.begin, start + n)),
+                         nxt)]
+            return []
+        pop.__name__ = f"pop{j}"
+        return pop
+
+    actors = [pusher(i) for i in range(len(pushes))] + [popper(j) for j in range(len(pops))]
+    pcs = tuple(["reserve"] * len(pushes) + [("wait", m) for m in pops])
+
+    def final(g, trace):
+        if sorted(g.out) != list(range(total)):
+            raise Violation(f"keys out {g.out}, pushed 0..{total - 1}", trace)
+        if g.begin != total or g.write != total or g.read != total:
+            raise Violation(f"positions end at read {g.read}, write {g.write}, begin {g.begin}", trace)
+
+    g0 = FifoState(slots=tuple([(-1, -1)] * capacity), end=0, write=0, read=0, begin=0, out=())
+    return (g0, pcs), actors, final

@@ -1,8 +1,9 @@
-"""Race detection for the heap's lock hand-offs, on CPU: every interleaving
-of the atomic steps of the bottom-up park protocol, of the top-down target
-hand-off and of the searches' termination protocol (oracle/lock_model.py)
-keeps its invariants and never deadlocks, and the explorer finds each planted mistake -- the ones these
-protocols exist to prevent -- with the interleaving that exposes it."""
+"""Race detection for the path's lock-free protocols, on CPU: every
+interleaving of the atomic steps of the bottom-up park protocol, the
+top-down target hand-off, the FIFO ring and the searches' termination
+protocol (oracle/lock_model.py) keeps its invariants and never deadlocks,
+and the explorer finds each planted mistake -- the ones these protocols
+exist to prevent -- with the interleaving that exposes it."""
 import pytest
 
 from oracle import lock_model as lm
@@ -109,3 +110,25 @@ def test_waiting_blocks_counted_busy_never_end():
     r = _run(lm.termination_model(count_while_waiting=True))
     assert r.deadlocks and r.finals == 0
     assert all("count self while waiting" in t for t in r.deadlocks[0][-2:])
+
+
+@pytest.mark.parametrize("pushes,pops,capacity", [((1, 1, 1), (1, 1, 1), 2), ((2, 1), (1, 2), 2),
+                                                   ((1, 1, 1), (2, 1), 1), ((2, 2), (3, 1), 2)])
+def test_fifo_protocol_is_safe(pushes, pops, capacity):
+    """gpuheap_fifo.cuh on a ring that wraps (down to one slot): no slot is
+    read before its push wrote it or after a later push overwrote it, every
+    key comes out once, and no interleaving leaves a block waiting."""
+    r = _run(lm.fifo_model(pushes=pushes, pops=pops, capacity=capacity))
+    assert r.finals >= 1 and not r.deadlocks
+
+
+@pytest.mark.parametrize("mistake,found", [("wait_room", "found (2, 2)"), ("publish_in_order", "found (-1, -1)"),
+                                           ("claim_by_cas", "found"), ("free_in_order", "found")])
+def test_fifo_planted_mistakes_are_caught(mistake, found):
+    """Each of the four waits and checks is needed: without the room wait a
+    push overwrites an unread slot, publishing out of order exposes an
+    unwritten one, a plain-store claim hands a position to two pops, and
+    freeing out of order lets a push overwrite a slot still being copied."""
+    with pytest.raises(lm.Violation, match="popper read slot") as e:
+        _run(lm.fifo_model(**{mistake: False}))
+    assert found in str(e.value)
