@@ -55,6 +55,7 @@ _SIGS = {
     "gh_heap_node_count": (_I, [_VP, ctypes.POINTER(_I)]),
     "gh_heap_is_empty": (_I, [_VP, ctypes.POINTER(_I)]),
     "gh_heap_snapshot": (_I, [_VP, _VP, _VP, _VP]),
+    "gh_heap_restore": (_I, [_VP, _VP, _VP]),
     "gh_heap_inject_lock": (_I, [_VP, _I, _I]),
     "gh_launch_count": (_LL, []),
     "gh_sort_noalloc": (_I, [_I, _I, _I, _I, _VP, _LL, _VP, _VP]),
@@ -392,6 +393,17 @@ class Heap:
         _check(lib().gh_heap_snapshot(self._h, items.ctypes.data, status.ctypes.data, counters.ctypes.data),
                "snapshot")
         return items, status, counters
+
+    def restore(self, items, counters):
+        """Puts back a snapshot's items and counters (from this heap or one of
+        the same shape) with every lock free and the error record cleared."""
+        import numpy as np
+        dt = {"u32": np.uint32, "i32": np.int32, "u64": np.uint64}[self.key]
+        items = np.ascontiguousarray(items, dt)
+        if items.size != (self.batch_num + 1) * self.batch_size:
+            raise ValueError(f"restore: {items.size} keys for a heap of {(self.batch_num + 1) * self.batch_size}")
+        c = np.ascontiguousarray(np.asarray(counters, np.int32)[:3])
+        _check(lib().gh_heap_restore(self._h, items.ctypes.data, c.ctypes.data), "restore")
 
     def inject_lock(self, node, state):
         """Fault injection: leave node's lock word in `state` (tests of the bounded waits)."""

@@ -520,6 +520,27 @@ gh_status gh_heap_snapshot(gh_heap* h, void* items_host, int* status_host, int* 
     return GH_OK;
 }
 
+gh_status gh_heap_restore(gh_heap* h, const void* items_host, const int* counters_host) {
+    if (!h || !items_host || !counters_host) return GH_ERR_INVALID;
+    const int bc = counters_host[0], ps = counters_host[1], dc = counters_host[2];
+    if (bc < 0 || bc > h->d.batchNum || ps < 0 || ps >= h->d.batchSize || (!h->d.pb && ps != 0) || dc < 0)
+        return GH_ERR_INVALID;
+    static_assert(offsetof(gh::HeapState, partialBufferSize) == offsetof(gh::HeapState, batchCount) + sizeof(int) &&
+                      offsetof(gh::HeapState, deleteCount) == offsetof(gh::HeapState, batchCount) + 2 * sizeof(int),
+                  "batchCount, partialBufferSize and deleteCount are adjacent");
+    GH_CUDA(cudaDeviceSynchronize());
+    GH_CUDA(cudaMemcpy(h->d.items, items_host, static_cast<size_t>(h->d.batchNum + 1) * h->d.batchSize * h->d.keyBytes,
+                       cudaMemcpyHostToDevice));
+    GH_CUDA(cudaMemset(h->d.status, 0, sizeof(int) * (static_cast<size_t>(h->d.batchNum) + 2)));
+    gh::impl::k_init_state<<<1, 32>>>(h->d.state, 0);
+    gh::impl::count_launch();
+    GH_CUDA(cudaGetLastError());
+    GH_CUDA(cudaDeviceSynchronize());
+    const int counters[3] = {bc, ps, dc};
+    GH_CUDA(cudaMemcpy(&h->d.state->batchCount, counters, sizeof(counters), cudaMemcpyHostToDevice));
+    return GH_OK;
+}
+
 gh_status gh_heap_inject_lock(gh_heap* h, int node, int state) {
     if (!h || node < 0 || node > h->d.batchNum) return GH_ERR_INVALID;
     GH_CUDA(cudaDeviceSynchronize());

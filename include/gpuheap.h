@@ -146,6 +146,15 @@ gh_status gh_heap_is_empty(gh_heap* h, int* empty);
  * batch_num + 1 lock words, counters_host {batchCount, partialBufferSize,
  * deleteCount, err, errOp, errNode, errState}.  Any pointer may be NULL. */
 gh_status gh_heap_snapshot(gh_heap* h, void* items_host, int* status_host, int* counters_host);
+/* Restores a heap from a snapshot taken with no operation in flight, by
+ * this heap or another of the same key kind, variant, partial-buffer flag,
+ * batch_num and batch_size: items_host holds (batch_num + 1) * batch_size
+ * keys, counters_host at least {batchCount, partialBufferSize,
+ * deleteCount}.  Every lock word becomes AVAIL and the error record, busy
+ * count and park tickets are cleared.  The reference has no counterpart
+ * (its nearest is Heap::reset, heap/tditdd/heap.cuh:69-91).  Synchronous;
+ * GH_ERR_INVALID when the counters do not fit this heap. */
+gh_status gh_heap_restore(gh_heap* h, const void* items_host, const int* counters_host);
 
 /* Fault injection from the host, for tests of the bounded waits: writes
  * `state` into the lock word of `node` (synchronously).  A lock word left

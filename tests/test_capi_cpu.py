@@ -86,3 +86,5 @@ def test_newer_entry_points_reject_bad_arguments(ghlib):
     assert ghlib.gh_batch_set_astar_blocks(None, 1 << 18, 8) == 1
     assert ghlib.gh_batch_set_timeout(None, 1.0) == 1
     assert ghlib.gh_serve_set_blocks(None, 1 << 15, 24, 1 << 18, 8) == 1
+    cnt = (ctypes.c_int * 3)(0, 0, 0)
+    assert ghlib.gh_heap_restore(None, ctypes.byref(t), cnt) == 1
