@@ -23,7 +23,6 @@ only): the oracle's std::sort of the same keys on all host cores.
 """
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
