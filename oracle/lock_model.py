@@ -108,7 +108,7 @@ BUState = namedtuple("BUState", "x p ver seen_i seen_i2 t_done in_heap")
 
 
 def bottomup_park_model(tagged=True, trust_own_park=True, delmod_on_release=True, with_taker=True,
-                        with_passer=True):
+                        with_passer=True, park_before_wait=True):
     """Node x with parent p.  Actors:
 
     * `ins` holds x (INUSE) with its batch cached; p is held by `holder`, so
@@ -126,7 +126,10 @@ def bottomup_park_model(tagged=True, trust_own_park=True, delmod_on_release=True
     ver is what it was at its park.  tagged=False parks every insert with
     the one value INSHOLD (the reference's protocol, which then must never
     trust); delmod_on_release=False restores the raw park value after a
-    pass-through."""
+    pass-through; park_before_wait=False makes the insert wait for p while
+    it still holds x, against a deleter that holds p and wants x (inserts
+    lock child then parent, deleters parent then child: the park is what
+    breaks that cycle)."""
     tag_i = PARK_BASE if tagged else INSHOLD
     tag_i2 = PARK_BASE + 1 if tagged else INSHOLD
 
@@ -137,7 +140,11 @@ def bottomup_park_model(tagged=True, trust_own_park=True, delmod_on_release=True
         if pc == "try_p":  # one attempt at the parent first
             if g.p == AVAIL:
                 return [("cas p ok", _set(g, p=INUSE), "own_p")]
+            if not park_before_wait:
+                return [("cas p fail; wait holding x", g, "lock_p_holding")]
             return [("cas p fail; park x", _set(g, x=tag_i, seen_i=g.ver), "lock_p")]
+        if pc == "lock_p_holding":
+            return [("lock p", _set(g, p=INUSE), "own_p")] if g.p == AVAIL else []
         if pc == "lock_p":
             return [("lock p", _set(g, p=INUSE), "retake")] if g.p == AVAIL else []
         if pc == "retake":  # atomicMax(x, INUSE), spinning while INUSE

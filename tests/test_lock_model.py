@@ -132,3 +132,14 @@ def test_fifo_planted_mistakes_are_caught(mistake, found):
     with pytest.raises(lm.Violation, match="popper read slot") as e:
         _run(lm.fifo_model(**{mistake: False}))
     assert found in str(e.value)
+
+
+def test_waiting_for_the_parent_without_parking_deadlocks():
+    """Inserts lock child then parent, sifting deleters parent then child:
+    an insert that waits for its parent while still holding its node
+    deadlocks against a deleter passing through (the park breaks the cycle);
+    with no deleter passing, the same insert finishes."""
+    r = _run(lm.bottomup_park_model(park_before_wait=False, with_taker=False))
+    assert r.deadlocks and r.deadlocks[0] == ["holder:sift toward x", "ins:cas p fail; wait holding x"]
+    r = _run(lm.bottomup_park_model(park_before_wait=False, with_taker=False, with_passer=False))
+    assert not r.deadlocks and r.finals == 1
