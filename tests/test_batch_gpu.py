@@ -123,10 +123,10 @@ def test_knapsack_orders_match_oracle(order, counter):
     order children reach the queue and the pool slots they get), so only
     their presence is checked: with a short counter at least one instance
     leaves the heap, and with a counter of 1 one also comes back from the
-    FIFO ring, over the two runs.  In a batch-synchronous model of these
-    instances (128 nodes a batch, best-first or oldest-first), a counter of
-    2 switches each of the four largest once and a counter of 1 three
-    times."""
+    FIFO ring, over the two runs.  In the batch-synchronous model of these
+    instances (oracle/knapsack_orders.py, pinned by
+    tests/test_knapsack_orders_cpu.py), a counter of 2 switches each of the
+    four largest once and a counter of 1 three times."""
     inst = small_mix(11)[:12] + knapsack_set(FIFO_SIZES)
     want = oracle_results(inst)
     kinds = np.array([k == "knapsack" for k, _ in inst])
