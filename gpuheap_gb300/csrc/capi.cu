@@ -14,6 +14,7 @@
 
 #include "gpuheap.h"
 #include "heap_launch.cuh"
+#include "trace.cuh"
 
 using gh::impl::Desc;
 
@@ -234,6 +235,7 @@ gh_status gh_heap_set_grid(gh_heap* h, int blocks) {
 }
 
 gh_status gh_heap_insert(gh_heap* h, const void* keys_dev, long long n, int chunk, void* stream) {
+    gh::trace::Range range_("gh_heap_insert");
     if (!h || n < 0 || (n > 0 && !keys_dev)) return GH_ERR_INVALID;
     if (chunk == 0) chunk = h->d.batchSize;
     if (chunk < 1 || chunk > h->d.batchSize) return GH_ERR_INVALID;
@@ -281,16 +283,19 @@ gh_status delete_bulk(gh_heap* h, void* out_dev, long long max_keys, const void*
 }  // namespace
 
 gh_status gh_heap_delete(gh_heap* h, void* out_dev, long long max_keys, long long* n_out, void* stream) {
+    gh::trace::Range range_("gh_heap_delete");
     return delete_bulk(h, out_dev, max_keys, nullptr, n_out, stream);
 }
 
 gh_status gh_heap_delete_below(gh_heap* h, void* out_dev, long long max_keys, const void* threshold,
                                long long* n_out, void* stream) {
+    gh::trace::Range range_("gh_heap_delete_below");
     if (!threshold) return GH_ERR_INVALID;
     return delete_bulk(h, out_dev, max_keys, threshold, n_out, stream);
 }
 
 gh_status gh_heap_gc(gh_heap* h, const void* threshold, long long* kept, void* stream) {
+    gh::trace::Range range_("gh_heap_gc");
     if (!h) return GH_ERR_INVALID;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // the used nodes, after the stream's work (the reference's invalidFilter
@@ -348,6 +353,7 @@ gh_status gh_heap_gc(gh_heap* h, const void* threshold, long long* kept, void* s
 
 gh_status gh_heap_concurrent(gh_heap* h, const void* keys_dev, long long n, int chunk, void* out_dev,
                              long long max_keys, long long* n_out, void* stream) {
+    gh::trace::Range range_("gh_heap_concurrent");
     if (!h || n < 0 || (n > 0 && !keys_dev) || max_keys < 0 || (max_keys > 0 && !out_dev)) return GH_ERR_INVALID;
     if (chunk == 0) chunk = h->d.batchSize;
     if (chunk < 1 || chunk > h->d.batchSize) return GH_ERR_INVALID;
@@ -405,6 +411,7 @@ gh_status gh_heap_delete_batch(gh_heap* h, void* out_dev, int* size, void* strea
 }
 
 gh_status gh_heap_retrieve(gh_heap* h, void* out_dev, int size, int* n_out, void* stream) {
+    gh::trace::Range range_("gh_heap_retrieve");
     if (!h || size < 0 || (size > 0 && !out_dev)) return GH_ERR_INVALID;
     if (!h->d.pb) return GH_ERR_INVALID;  // the remainder goes back through the partial buffer
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -422,6 +429,7 @@ gh_status gh_heap_retrieve(gh_heap* h, void* out_dev, int size, int* n_out, void
 }
 
 gh_status gh_heap_sort(gh_heap* h, const void* in_dev, long long n, void* out_dev, void* stream) {
+    gh::trace::Range range_("gh_heap_sort");
     if (!h || n < 0 || (n > 0 && (!in_dev || !out_dev))) return GH_ERR_INVALID;
     if (n > static_cast<long long>(h->d.batchNum) * h->d.batchSize) return GH_ERR_CAPACITY;
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -13,6 +13,7 @@
 #include "gpuheap_fifo.cuh"
 #include "gpuheap_fifo.h"
 #include "heap_kernels.cuh"
+#include "trace.cuh"
 
 namespace gh {
 namespace impl {
@@ -339,6 +340,7 @@ gh_status gh_fifo_set_launch(gh_fifo* f, int blocks, int threads) {
 }
 
 gh_status gh_fifo_push(gh_fifo* f, const void* keys_dev, long long n, int chunk, void* stream) {
+    gh::trace::Range range_("gh_fifo_push");
     if (!f || n < 0 || (n > 0 && !keys_dev) || chunk < 0) return GH_ERR_INVALID;
     if (static_cast<unsigned long long>(chunk) > f->capacity) return GH_ERR_INVALID;
     if (f->errSeen) return GH_ERR_STATE;
@@ -389,6 +391,7 @@ gh_status gh_fifo_push(gh_fifo* f, const void* keys_dev, long long n, int chunk,
 }
 
 gh_status gh_fifo_pop(gh_fifo* f, void* out_dev, long long max_keys, int chunk, long long* n_out, void* stream) {
+    gh::trace::Range range_("gh_fifo_pop");
     if (!f || max_keys < 0 || (max_keys > 0 && !out_dev) || chunk < 0) return GH_ERR_INVALID;
     if (f->errSeen) return GH_ERR_STATE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -441,6 +444,7 @@ gh_status gh_fifo_pop(gh_fifo* f, void* out_dev, long long max_keys, int chunk, 
 
 gh_status gh_fifo_concurrent(gh_fifo* f, const void* keys_dev, long long n, int chunk, void* out_dev,
                              long long max_keys, long long* n_out, void* stream) {
+    gh::trace::Range range_("gh_fifo_concurrent");
     if (!f || n < 0 || (n > 0 && !keys_dev) || max_keys < 0 || (max_keys > 0 && !out_dev) || chunk < 0)
         return GH_ERR_INVALID;
     if (chunk == 0) chunk = static_cast<int>(std::min<unsigned long long>(1024, f->capacity));

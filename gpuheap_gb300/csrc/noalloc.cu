@@ -17,6 +17,7 @@
 
 #include "gpuheap.h"
 #include "heap_launch.cuh"
+#include "trace.cuh"
 
 namespace {
 
@@ -75,6 +76,7 @@ cudaError_t run_sort(const gh::impl::Desc& d, const void* in, long long n, void*
 
 extern "C" gh_status gh_sort_noalloc(int key_kind, int variant, int partial_buffer, int batch_size,
                                      const void* in_dev, long long n, void* out_dev, void* stream) {
+    gh::trace::Range range_("gh_sort_noalloc");
     if (key_kind < GH_KEY_U32 || key_kind > GH_KEY_U64) return GH_ERR_INVALID;
     if (variant != GH_TOPDOWN && variant != GH_BOTTOMUP) return GH_ERR_INVALID;
     if (batch_size < 16 || batch_size > 4096 || (batch_size & (batch_size - 1))) return GH_ERR_INVALID;

@@ -39,6 +39,7 @@
 
 #include "gpuheap.h"
 #include "search_kernels.cuh"
+#include "trace.cuh"
 
 // ---------------------------------------------------------------------- host side
 struct HostInst {
@@ -366,6 +367,7 @@ gh_status gh_batch_build(gh_batch* b, void* stream) {
 // GH_BATCH_GRAPH: the same, replayed from a captured CUDA graph;
 // GH_BATCH_PLAIN: one launch per instance, back to back.
 gh_status gh_batch_run(gh_batch* b, int mode, void* stream) {
+    gh::trace::Range range_("gh_batch_run");
     if (!b || !b->built) return GH_ERR_INVALID;
     if (mode != GH_BATCH_PERSISTENT && mode != GH_BATCH_GRAPH && mode != GH_BATCH_PLAIN) return GH_ERR_INVALID;
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -26,6 +26,7 @@
 
 #include "gpuheap.h"
 #include "search_kernels.cuh"
+#include "trace.cuh"
 
 namespace {
 
@@ -309,6 +310,7 @@ gh_status gh_serve_submit(gh_server* s, int kind, int dataset, int a, int b, lon
 }
 
 gh_status gh_serve_step(gh_server* s, void* stream, int* finished, int* active, int* queued) {
+    gh::trace::Range range_("gh_serve_step");
     if (!s) return GH_ERR_INVALID;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     s->finished.clear();

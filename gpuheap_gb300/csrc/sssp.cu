@@ -21,6 +21,7 @@
 #include "heap_launch.cuh"
 #include "sssp_relax.cuh"
 #include "worklist.cuh"
+#include "trace.cuh"
 
 struct gh_heap;  // defined in capi.cu; reached through gh_heap_device_view
 
@@ -151,6 +152,7 @@ extern "C" gh_status gh_rmat_edges(int scale, long long m, double a, double b, d
 
 extern "C" gh_status gh_sssp(gh_heap* h, int n, const long long* rowptr_dev, const int* col_dev, const unsigned* w_dev,
                              int source, unsigned* dist_dev, void* stream, unsigned long long* stats_host) {
+    gh::trace::Range range_("gh_sssp");
     if (!h || n < 1 || !rowptr_dev || !col_dev || !w_dev || !dist_dev || source < 0 || source >= n) return GH_ERR_INVALID;
     int kind = 0, variant = 0, pb = 0, bn = 0, B = 0, threads = 0, grid = 0;
     gh_status st = gh_heap_info(h, &kind, &variant, &pb, &bn, &B, &threads, &grid);
