@@ -57,7 +57,7 @@ def build(verbose=False):
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
     if _stale(LIB, objs):
-        cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-ldl"]  # NVTX finds its tool by dlopen
+        cmd = [_nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
