@@ -276,6 +276,19 @@ def workload_config(args):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+def owner_summary(st, sm_mhz):
+    """Per-delete breakdown of the owner-mode bulk delete of the last step
+    (device SM-cycle counters / the SM clock sampled during the run)."""
+    d = st.get("deletes", 0)
+    if not d:
+        return None
+    mhz = sm_mhz or 2070.0
+    us = lambda k: round(st[k] / d / mhz, 3)
+    return {"deletes": d, "lends": st["lends"], "reloads": st["reloads"], "general_steps": st["general_steps"],
+            "us_per_delete": {k: us(k) for k in ("loop", "wait_carried", "wait_lent", "wait_ring", "plan", "pass")},
+            "taker_us_per_delete": {k: us(k) for k in ("take_lock", "take_load", "take_idle")}}
+
+
 # ------------------------------------------------------------------ our arm
 def our_arm(args):
     import torch
@@ -391,6 +404,7 @@ def our_arm(args):
                "ms_per_step": round(e2e_ms / args.steps, 3),
                "path": "pinned host keys -> cudaMemcpyAsync -> gh_heap_sort -> pinned host output"}
 
+    owner = owner_summary(h.owner_stats(), clk.summary().get("sm_mhz"))
     value = job_rate(n, ws, args.steps, total_ms)
     ins_b, del_b = algorithmic_bytes(n, B, s, pb)
     ti, td = statistics.mean(t_ins), statistics.mean(t_del)
@@ -410,6 +424,7 @@ def our_arm(args):
         "config": dict(workload_config(args), block_threads=info["block_threads"], grid=info["grid"]),
         "phases_ms": {"reset": round(statistics.mean(t_reset), 3), "insert": round(ti, 3), "delete": round(td, 3)},
         "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
+        "owner_delete": owner,
         "whole_sort_bytes_per_key": round((ins_b + del_b) / n, 2),
         "io_lower_bound_bytes_per_key": 2 * s,
     }

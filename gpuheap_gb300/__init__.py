@@ -58,6 +58,7 @@ _SIGS = {
     "gh_heap_restore": (_I, [_VP, _VP, _VP]),
     "gh_heap_inject_lock": (_I, [_VP, _I, _I]),
     "gh_launch_count": (_LL, []),
+    "gh_heap_owner_stats": (_I, [_VP, _VP, _I]),
     "gh_sort_noalloc": (_I, [_I, _I, _I, _I, _VP, _LL, _VP, _VP]),
     "gh_gen_keys": (_I, [_I, _I, ctypes.c_ulonglong, _LL, _VP, _VP]),
     "gh_rmat_edges": (_I, [_I, _LL, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong,
@@ -404,6 +405,16 @@ class Heap:
             raise ValueError(f"restore: {items.size} keys for a heap of {(self.batch_num + 1) * self.batch_size}")
         c = np.ascontiguousarray(np.asarray(counters, np.int32)[:3])
         _check(lib().gh_heap_restore(self._h, items.ctypes.data, c.ctypes.data), "restore")
+
+    OWNER_STATS = ("deletes", "wait_carried", "wait_lent", "wait_ring", "plan", "pass", "general_steps", "loop",
+                   "take_lock", "take_load", "take_idle", "lends", "reloads")
+
+    def owner_stats(self):
+        """Counters of the last owner-mode bulk delete (SM cycles unless a count)."""
+        import numpy as np
+        buf = np.zeros(len(self.OWNER_STATS), np.uint64)
+        _check(lib().gh_heap_owner_stats(self._h, buf.ctypes.data, buf.size), "owner_stats")
+        return dict(zip(self.OWNER_STATS, (int(v) for v in buf)))
 
     def inject_lock(self, node, state):
         """Fault injection: leave node's lock word in `state` (tests of the bounded waits)."""

@@ -185,6 +185,10 @@ gh_status gh_heap_create(gh_heap** out, int key_kind, int variant, int partial_b
     if (cudaMalloc(&h->check, sizeof(gh::impl::CheckResult)) != cudaSuccess) { cudaGetLastError(); return fail(GH_ERR_CUDA); }
     if (cudaMalloc(&h->opSize, sizeof(int)) != cudaSuccess) { cudaGetLastError(); return fail(GH_ERR_CUDA); }
     if (cudaMalloc(&h->scratch, static_cast<size_t>(batch_size) * kb) != cudaSuccess) { cudaGetLastError(); return fail(GH_ERR_CUDA); }
+    if (gh::impl::owner_depth(batch_size, kb) > 0) {
+        if (cudaMalloc(&h->d.mbox, gh::impl::mbox_bytes(batch_size, kb)) != cudaSuccess) { cudaGetLastError(); return fail(GH_ERR_CUDA); }
+        if (cudaMemset(h->d.mbox, 0, sizeof(gh::impl::Mailbox)) != cudaSuccess) { cudaGetLastError(); return fail(GH_ERR_CUDA); }
+    }
     gh_status st = fill_items(h, nullptr);
     if (st != GH_OK) return fail(st);
     if (cudaDeviceSynchronize() != cudaSuccess) return fail(GH_ERR_CUDA);
@@ -200,6 +204,7 @@ gh_status gh_heap_destroy(gh_heap* h) {
     if (h->check) cudaFree(h->check);
     if (h->opSize) cudaFree(h->opSize);
     if (h->scratch) cudaFree(h->scratch);
+    if (h->d.mbox) cudaFree(h->d.mbox);
     delete h;
     return GH_OK;
 }
@@ -388,6 +393,7 @@ gh_status gh_heap_insert_batch(gh_heap* h, const void* keys_dev, int size, void*
     if (size == 0) return GH_OK;
     gh::impl::LaunchArgs a = args_of(h, static_cast<cudaStream_t>(stream));
     a.grid = 1;
+    a.reserve = false;  // one insertion() call, node 0 and all, as the reference makes it
     return with_key(h, [&](auto k) {
         using K = decltype(k);
         return gh::impl::launch_insert<K>(a, static_cast<const K*>(keys_dev), size, size);
@@ -557,6 +563,17 @@ gh_status gh_heap_inject_lock(gh_heap* h, int node, int state) {
 }
 
 long long gh_launch_count(void) { return gh::impl::g_launches.load(); }
+
+gh_status gh_heap_owner_stats(gh_heap* h, unsigned long long* out, int n) {
+    if (!h || n < 0 || (n > 0 && !out)) return GH_ERR_INVALID;
+    const int m = std::min(n, static_cast<int>(gh::impl::kStCount));
+    for (int i = 0; i < n; ++i) out[i] = 0;
+    if (!h->d.mbox || m == 0) return GH_OK;
+    GH_CUDA(cudaDeviceSynchronize());
+    const auto* mb = static_cast<const gh::impl::Mailbox*>(h->d.mbox);
+    GH_CUDA(cudaMemcpy(out, mb->stats, sizeof(unsigned long long) * m, cudaMemcpyDeviceToHost));
+    return GH_OK;
+}
 
 size_t gh_heap_view_bytes(void) { return 64; }
 static_assert(sizeof(gh::Heap<uint64_t, 0, true>) <= 64, "device view size");

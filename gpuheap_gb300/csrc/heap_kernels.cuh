@@ -28,6 +28,7 @@ struct Desc {
     int variant;
     int pb;
     int keyBytes;
+    void* mbox;  // owner-mode bulk delete: mailbox + lend buffers (null: plain deleteKernel only)
 };
 
 // insertKernel: chunks of `chunk` keys, grid-strided over blocks.
@@ -39,6 +40,43 @@ __global__ void __launch_bounds__(1024) k_insert(H h, const K* __restrict__ keys
         const long long rem = n - off;
         const int size = rem < chunk ? static_cast<int>(rem) : chunk;
         h.insertion(keys + off, size, 0);
+        if (h.failed()) return;
+    }
+}
+
+// Bulk insert of `m` full batches, step 1 (one thread): with the partial
+// buffer empty, no error recorded and room for all of them, reserve targets
+// batchCount+1 .. batchCount+m (batchCount moves past them now, as m
+// node-0 hand-offs would have moved it); otherwise reserve nothing and the
+// insert kernel takes node 0 per batch as the reference does.
+static __global__ void k_reserve(HeapState* st, int batchNum, long long m) {
+    const int bc = st->batchCount;
+    const bool ok = m > 0 && st->err == 0 && st->partialBufferSize == 0 && bc + m <= batchNum;
+    st->resvBase = bc;
+    st->resvCount = ok ? static_cast<int>(m) : 0;
+    st->resvTurn = bc + 1;
+    if (ok) st->batchCount = bc + static_cast<int>(m);
+}
+
+// Step 2: the reserved targets' lock words take the state an insert holds
+// its target in (top-down TARGET, bottom-up INUSE), so that an insert that
+// reaches one before its own insert has written it waits there.
+static __global__ void k_mark_reserved(const HeapState* st, int* status, int held) {
+    const int base = st->resvBase, cnt = st->resvCount;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) status[base + 1 + i] = held;
+}
+
+// Step 3: insertKernel over the full batches; batch i goes to reserved
+// target resvBase + 1 + i (batches in increasing order per block, so a
+// block never waits on a target that it inserts later itself).  Without a
+// reservation, insertion() as in k_insert.
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_insert_reserved(H h, const K* __restrict__ keys, long long m) {
+    const int base = h.state->resvBase, cnt = h.state->resvCount;
+    for (long long i = blockIdx.x; i < m; i += gridDim.x) {
+        const K* src = keys + i * h.batchSize;
+        if (cnt) h.insertionReserved(src, base + 1 + static_cast<int>(i), 0);
+        else h.insertion(src, h.batchSize, 0);
         if (h.failed()) return;
     }
 }
@@ -126,6 +164,9 @@ static __global__ void k_init_state(HeapState* st, int deleteCount) {
         st->deleteCount = deleteCount;
         st->outLimit = INT_MAX;
         st->insTicket = 0;
+        st->resvBase = 0;
+        st->resvCount = 0;
+        st->resvTurn = 0;
         st->err = 0;
         st->errOp = 0;
         st->errNode = 0;

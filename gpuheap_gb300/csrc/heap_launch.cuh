@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "heap_kernels.cuh"
+#include "owner_delete.cuh"
 
 namespace gh {
 namespace impl {
@@ -16,6 +17,7 @@ struct LaunchArgs {
     int grid;
     cudaStream_t stream;
     int* opSize;
+    bool reserve = true;  // bulk inserts of full batches may reserve their targets (k_reserve)
 };
 
 template <typename K>
@@ -78,17 +80,38 @@ inline H view_of(const Desc& d, int sortOutput) {
     return h;
 }
 
+// Full batches (chunk == batchSize) go to targets reserved up front when the
+// partial buffer is empty (k_reserve, k_mark_reserved, k_insert_reserved);
+// a ragged last chunk, or any other chunk size, goes through insertion().
 template <typename K>
 cudaError_t launch_insert(const LaunchArgs& a, const K* keys, long long n, int chunk) {
     return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
         using H = decltype(proto);
         const H h = view_of<H>(*a.d, 1);
-        const size_t smem = H::smemBytes(a.d->batchSize);
+        const int B = a.d->batchSize;
+        const size_t smem = H::smemBytes(B);
+        const long long m = (a.reserve && chunk == B) ? n / B : 0;
+        if (m > 0) {
+            cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_insert_reserved<H, K>), smem);
+            if (e != cudaSuccess) return e;
+            k_reserve<<<1, 1, 0, a.stream>>>(a.d->state, a.d->batchNum, m);
+            count_launch();
+            const int held = a.d->variant == kTopDown ? TD::TARGET : BU::INUSE;
+            const long long mb = (m + 255) / 256;
+            k_mark_reserved<<<static_cast<int>(mb < 1024 ? mb : 1024), 256, 0, a.stream>>>(a.d->state, a.d->status, held);
+            count_launch();
+            k_insert_reserved<H, K><<<static_cast<int>(m < a.grid ? m : a.grid), a.threads, smem, a.stream>>>(h, keys, m);
+            count_launch();
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        const long long rest = n - m * B;
+        if (rest <= 0) return cudaSuccess;
         cudaError_t e = allow_smem<H>(reinterpret_cast<const void*>(k_insert<H, K>), smem);
         if (e != cudaSuccess) return e;
-        const long long nchunks = (n + chunk - 1) / chunk;
+        const long long nchunks = (rest + chunk - 1) / chunk;
         const int g = static_cast<int>(nchunks < a.grid ? nchunks : a.grid);
-        k_insert<H, K><<<g, a.threads, smem, a.stream>>>(h, keys, n, chunk);
+        k_insert<H, K><<<g, a.threads, smem, a.stream>>>(h, keys + m * B, rest, chunk);
         count_launch();
         return cudaGetLastError();
     });
@@ -108,8 +131,30 @@ cudaError_t launch_insert_counted(const LaunchArgs& a, const K* keys, const unsi
     });
 }
 
+// Without a threshold, a heap with a mailbox first runs the owner-mode bulk
+// delete (k_delete_owner, 1024-thread blocks) while it has nodes below its
+// resident levels, then deleteKernel finishes; with a threshold,
+// deleteKernel alone.
 template <typename K>
 cudaError_t launch_erase(const LaunchArgs& a, K* out, const K* threshold) {
+    const int R = owner_depth(a.d->batchSize, a.d->keyBytes);
+    if (!threshold && a.d->mbox && R > 0 && a.grid >= 2) {
+        cudaError_t e = cudaMemsetAsync(a.d->mbox, 0, sizeof(Mailbox), a.stream);
+        if (e != cudaSuccess) return e;
+        e = dispatch<K>(*a.d, 1024, [&](auto proto) -> cudaError_t {
+            using H = decltype(proto);
+            const H h = view_of<H>(*a.d, 1);
+            const size_t smem = owner_smem(a.d->batchSize, a.d->keyBytes, R);
+            cudaError_t e2 = allow_smem<H>(reinterpret_cast<const void*>(k_delete_owner<H, K>), smem);
+            if (e2 != cudaSuccess) return e2;
+            Mailbox* mb = static_cast<Mailbox*>(a.d->mbox);
+            K* mdata = reinterpret_cast<K*>(static_cast<char*>(a.d->mbox) + sizeof(Mailbox));
+            k_delete_owner<H, K><<<a.grid, 1024, smem, a.stream>>>(h, out, mb, mdata, R);
+            count_launch();
+            return cudaGetLastError();
+        });
+        if (e != cudaSuccess) return e;
+    }
     return dispatch<K>(*a.d, a.threads, [&](auto proto) -> cudaError_t {
         using H = decltype(proto);
         const H h = view_of<H>(*a.d, 1);

@@ -1,0 +1,751 @@
+// Bulk delete with the top of the heap held in one block's shared memory.
+//
+// The reference's deleteKernel (test/heap_test.cu:60-77) has every block
+// call deleteRoot/deleteUpdate (heap/tditdd/heap.cuh:267-534,
+// heap/buitdd/heap.cuh:283-482) in a loop; consecutive deletes then follow
+// each other down the heap two levels apart, and each level step pays an L2
+// lock, a node load and a release fence (about 3 us on GB300), so the root
+// is handed on every ~6 us.  Here the same deletes run in the same order
+// with the same node updates, but:
+//
+//   * block 0, the owner, keeps node 0 (partial buffer) and levels 0..R of
+//     the heap (nodes 1 .. 2^(R+1)-1) in shared memory for the whole launch
+//     and holds their lock words; no other block touches those nodes;
+//   * a delete's sift steps at levels 0..R-1 only read the children's last
+//     keys to pick the path and only merge children into their parent, so
+//     once the path is known they are independent: the owner plans the
+//     path (one thread), then merges every level of it at once (29 warps);
+//   * the sift continues below level R in a worker block (every other block
+//     of the launch): the owner lends it the level-R node on the path
+//     together with the carried batch through a mailbox in global memory,
+//     and the worker runs deleteUpdate's sift loop from there with the
+//     usual locks; when the worker releases that node, the owner takes it
+//     back and reloads it;
+//   * three control warps of the owner overlap the global latency with the
+//     merges: one takes the next delete's last node (lock, bulk load, reset
+//     to init_limits, release), one copies lends into the mailbox, one
+//     takes lent nodes back.
+//
+// The owner stops when the output limit is reached or the heap has too few
+// nodes left for its resident levels; it then writes those levels back to
+// their global nodes, restores the counters and releases the lock words,
+// and the caller finishes with k_delete.  Every wait is bounded by the
+// heap's time limit; on expiry the heap's sticky error is raised and every
+// role stops at its next check.
+#pragma once
+#include <climits>
+#include <cstdint>
+
+#include "heap_kernels.cuh"
+
+namespace gh {
+namespace impl {
+
+constexpr int kMboxEntries = 32;   // lends in flight between owner and workers
+constexpr int kOwnerWarps = 29;    // compute warps of the owner block
+constexpr int kOwnerIpt = 16;      // keys per lane of a merge window (window = 512 keys)
+constexpr int kOwnerMaxR = 4;      // deepest resident level
+
+// Mailbox in global memory: lend q (q = 0, 1, ...) sits in entry q % 32 with
+// its carried batch at data + entry * batchSize.
+struct alignas(128) Mailbox {
+    int claim;  // next lend number a worker takes
+    int pad0[31];
+    int done;   // the owner posts no lend numbered >= total
+    int total;
+    int pad1[30];
+    int seq[kMboxEntries];   // entry e holds lend q once seq[e] == q + 1
+    int cons[kMboxEntries];  // uses of entry e that a worker has read
+    int node[kMboxEntries];  // the level-R node lent with it
+    unsigned long long stats[16];  // counters of the launch, indexed by OwnerStat
+};
+
+// Indices of Mailbox::stats (SM cycles unless a count).
+enum OwnerStat : int {
+    kStDeletes = 0,     // deletes made by the owner
+    kStWaitCarried,     // compute: waiting for the taker's last node
+    kStWaitLent,        // compute: waiting for a lent level-R node to come back
+    kStWaitRing,        // compute: waiting for room in the lend ring
+    kStPlan,            // compute: path plans
+    kStPass,            // compute: merge passes, general steps included
+    kStGeneral,         // general sift steps (count)
+    kStLoop,            // compute: the whole delete loop
+    kStTakeLock,        // taker: last-node lock waits
+    kStTakeLoad,        // taker: last-node bulk loads
+    kStTakeIdle,        // taker: waiting for permission or a free buffer
+    kStLends,           // lends posted (count)
+    kStReloads,         // lent nodes taken back (count)
+    kStCount = 16
+};
+
+// Shared-memory control words of the owner block (after its node slots).
+struct alignas(16) OwnerCtl {
+    unsigned long long cbar[2];                 // bulk loads of the two carried-batch buffers
+    unsigned long long rbar[1 << kOwnerMaxR];   // bulk reloads of lent level-R nodes
+    unsigned long long sbar;                    // set-up loads
+    int cReady[2];     // buffer b holds the last node of delete t once cReady[b] == t + 1
+    int cFree[2];      // uses of buffer b finished (lent out or done with)
+    int cEnd;          // delete number the taker found no last node for, else -1
+    int takeAllowed;   // the taker may take last nodes for deletes < takeAllowed
+    int lentState[1 << kOwnerMaxR];  // level-R node 2^R + i: 0 in its slot, 1 lent out, 2 lost (error)
+    int reqNode[4], reqBuf[4];       // lend requests, ring of 4
+    int lendReq;       // requests posted
+    int lendDone;      // requests copied out
+    int stop;          // compute warps are done; the control warps finish
+    int bcFinal;       // batch count after the taker's last take
+    int engaged;       // set-up outcome
+    int bc0, ps, dc0, lim;
+    // plan of one segment (compute thread 0 -> compute warps)
+    int plStop, nm, gen, genL, genR, genLarger, genSmaller, lend;
+    int mA[kOwnerMaxR], mB[kOwnerMaxR], mLo[kOwnerMaxR], mHi[kOwnerMaxR];
+    int caseSel;
+};
+
+// Resident depth R for a batch size and key size (0: no owner mode): the
+// deepest R <= 4 whose 2^(R+1) + 3 node slots fit in 200 KB of shared memory
+// and whose R merges fit the compute warps.
+inline int owner_depth(int batchSize, int keyBytes) {
+    if (batchSize < 512 || 2 * batchSize / 1024 > 8) return 0;
+    for (int R = kOwnerMaxR; R >= 2; --R) {
+        const size_t bytes = static_cast<size_t>((2 << R) + 3) * batchSize * keyBytes + sizeof(OwnerCtl);
+        const int windows = R * (2 * batchSize / (32 * kOwnerIpt));
+        if (bytes <= 200 * 1024 && windows <= kOwnerWarps) return R;
+    }
+    return 0;
+}
+// Bytes of the mailbox and its lend buffers for a heap.
+inline size_t mbox_bytes(int batchSize, int keyBytes) {
+    return sizeof(Mailbox) + static_cast<size_t>(kMboxEntries) * batchSize * keyBytes;
+}
+inline size_t owner_smem(int batchSize, int keyBytes, int R) {
+    return static_cast<size_t>((2 << R) + 3) * batchSize * keyBytes + sizeof(OwnerCtl);
+}
+
+namespace ow {
+
+__device__ __forceinline__ void bar_compute() {
+    asm volatile("bar.sync 1, %0;" ::"r"(kOwnerWarps * 32) : "memory");
+}
+__device__ __forceinline__ int lds_acq(const int* p) {
+    int v;
+    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(detail::smem_u32(p)) : "memory");
+    return v;
+}
+__device__ __forceinline__ void sts_rel(int* p, int v) {
+    asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(detail::smem_u32(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ void stg_rel(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int level_of(int i) { return 31 - __clz(i); }
+
+template <typename K>
+__device__ __forceinline__ K key_max() {
+    if constexpr (sizeof(K) == 8) return static_cast<K>(~0ull);
+    else if constexpr (static_cast<K>(-1) < static_cast<K>(0)) return static_cast<K>(0x7fffffff);
+    else return static_cast<K>(0xffffffffu);
+}
+
+// Start of the merge-path split at output diagonal D of sorted a[0,n) and
+// b[0,n): the number of a's keys among the first D outputs (a wins ties).
+// The warp probes 32 positions per round at an odd stride, so the probes of
+// one round fall in 32 different banks; three rounds cover n = 2048.
+template <typename K>
+__device__ __forceinline__ int warp_split(const K* a, const K* b, int n, int D) {
+    const int lane = threadIdx.x & 31;
+    int L = D > n ? D - n : 0, H = D < n ? D : n;
+    while (H > L) {
+        const int step = ((H - L + 31) >> 5) | 1;
+        const int p = L + (lane + 1) * step - 1;
+        const bool t = p < H && a[p] <= b[D - 1 - p];
+        const int c = __popc(__ballot_sync(0xffffffffu, t));
+        const int nh = L + (c + 1) * step - 1;
+        L = c == 0 ? L : L + c * step;
+        H = nh < H ? nh : H;
+    }
+    return L;
+}
+
+// One merge window: outputs [D, D + 32*IPT) of merge(a, b) into m, element
+// k = r*32 + lane in m[r].  The window's keys are the 32*IPT smallest of
+// a[i0, i0+S) and b[j0, j0+S): min(x_k, y_{S-1-k}) is that set as a
+// bitonic sequence, sorted by a bitonic network (strides >= 32 inside the
+// registers, < 32 across lanes).  Reads only shared memory.
+template <typename K, int IPT>
+__device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (&m)[IPT]) {
+    constexpr int S = 32 * IPT;
+    const int lane = threadIdx.x & 31;
+    const int i0 = warp_split(a, b, n, D), j0 = D - i0;
+    const K top = key_max<K>();
+#pragma unroll
+    for (int r = 0; r < IPT; ++r) {
+        const int k = r * 32 + lane;
+        const int xi = i0 + k, yi = j0 + (S - 1 - k);
+        const K x = xi < n ? a[xi] : top;
+        const K y = yi < n ? b[yi] : top;
+        m[r] = x < y ? x : y;
+    }
+#pragma unroll
+    for (int s = IPT / 2; s > 0; s >>= 1) {
+#pragma unroll
+        for (int r = 0; r < IPT; ++r)
+            if ((r & s) == 0) {
+                const K u = m[r], v = m[r + s];
+                m[r] = u < v ? u : v;
+                m[r + s] = u < v ? v : u;
+            }
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        const bool upper = (lane & s) != 0;
+#pragma unroll
+        for (int r = 0; r < IPT; ++r) {
+            const K o = __shfl_xor_sync(0xffffffffu, m[r], s);
+            m[r] = upper ? (m[r] > o ? m[r] : o) : (m[r] < o ? m[r] : o);
+        }
+    }
+}
+template <typename K, int IPT>
+__device__ __forceinline__ void window_store(K* lo, K* hi, int n, int D, const K (&m)[IPT]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < IPT; ++r) {
+        const int o = D + r * 32 + lane;
+        if (o < n) lo[o] = m[r];
+        else hi[o - n] = m[r];
+    }
+}
+
+// Posts lend request (node, buffer) to the lender warp; compute thread 0.
+__device__ __forceinline__ void post_lend(OwnerCtl* oc, int node, int buf) {
+    const int q = oc->lendReq;
+    oc->reqNode[q & 3] = node;
+    oc->reqBuf[q & 3] = buf;
+    sts_rel(&oc->lendReq, q + 1);
+}
+
+}  // namespace ow
+
+// ---------------------------------------------------------------- workers
+// Blocks 1.. of the launch: take lends in order, load the carried batch and
+// run deleteUpdate's sift from the lent node (heap/tditdd/heap.cuh:418-532,
+// heap/buitdd/heap.cuh:403-480), which releases that node after its first
+// level -- the owner's signal that it can take it back.
+template <typename H, typename K>
+__device__ void owner_worker(const H& h, Mailbox* mb, const K* mdata) {
+    K* base = h.region(0);
+    const int B = h.batchSize;
+    __shared__ int w_node, w_entry, w_q, w_exit;
+    for (;;) {
+        typename H::Op op(&h, h.ctl(base));
+        if (threadIdx.x == 0) {
+            const int q = atomicAdd(&mb->claim, 1);
+            const int e = q % kMboxEntries;
+            int ex = 0;
+            unsigned long long t0 = 0;
+            for (unsigned it = 0;; ++it) {
+                if (detail::ld_acquire(&mb->seq[e]) == q + 1) break;
+                if (detail::ld_acquire(&mb->done) && q >= detail::ld_relaxed(&mb->total)) { ex = 1; break; }
+                if (!h.keep_waiting(t0, it, kSiteHandOff, -1, q)) { ex = 1; break; }
+                __nanosleep(64);
+            }
+            w_exit = ex;
+            w_q = q;
+            w_entry = e;
+            if (!ex) {
+                w_node = detail::ld_relaxed(&mb->node[e]);
+                op.issue(h.nodeBytes());
+                detail::bulk_g2s(base, mdata + static_cast<size_t>(e) * B, h.nodeBytes(), &op.c->bar);
+            }
+        }
+        __syncthreads();
+        if (w_exit) return;
+        if (!op.wait()) return;
+        if (threadIdx.x == 0) ow::stg_rel(&mb->cons[w_entry], w_q / kMboxEntries + 1);
+        h.sift_loop(op, w_node, 0, base, base + 2 * B, base + 3 * B);
+        if (h.failed()) return;
+    }
+}
+
+// ---------------------------------------------------------------- owner
+template <typename H, typename K>
+__device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
+    extern __shared__ __align__(16) unsigned char gh_dyn_smem[];
+    constexpr int IPT = kOwnerIpt;
+    constexpr int S = 32 * IPT;
+    const int B = h.batchSize;
+    const int NR = (2 << R) - 1;       // resident nodes 1..NR; node i in slot i-1
+    const int firstR = 1 << R;         // level-R nodes firstR .. NR
+    const int sP = NR, sC = NR + 1, sT = NR + 3;
+    K* slots = reinterpret_cast<K*>(gh_dyn_smem);
+    OwnerCtl* oc = reinterpret_cast<OwnerCtl*>(slots + static_cast<size_t>(NR + 4) * B);
+    auto slot = [&](int s) -> K* { return slots + static_cast<size_t>(s) * B; };
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned nb = h.nodeBytes();
+    constexpr int L = H::lockedState();
+
+    // ---- set-up: every thread of the block
+    if (tid == 0) {
+        oc->cReady[0] = oc->cReady[1] = 0;
+        oc->cFree[0] = oc->cFree[1] = 0;
+        oc->cEnd = -1;
+        oc->lendReq = oc->lendDone = 0;
+        oc->stop = 0;
+        oc->plStop = 0;
+        for (int i = 0; i < (1 << kOwnerMaxR); ++i) oc->lentState[i] = 0;
+        const int bc = detail::ld_relaxed(&h.state->batchCount);
+        oc->bc0 = bc;
+        oc->ps = detail::ld_relaxed(&h.state->partialBufferSize);
+        oc->dc0 = detail::ld_relaxed(&h.state->deleteCount);
+        oc->lim = detail::ld_relaxed(&h.state->outLimit);
+        oc->bcFinal = bc;
+        oc->engaged = detail::ld_relaxed(&h.state->err) == 0 && bc >= (2 << R) + 1 &&
+                      static_cast<long long>(oc->dc0) + B <= oc->lim;
+        oc->takeAllowed = 1;
+        detail::mbar_init(&oc->cbar[0], 1);
+        detail::mbar_init(&oc->cbar[1], 1);
+        detail::mbar_init(&oc->sbar, 1);
+        for (int i = 0; i < (1 << kOwnerMaxR); ++i) detail::mbar_init(&oc->rbar[i], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (oc->engaged && warp == 0) {
+        // hold node 0 and every resident node: nobody else uses the heap during a bulk delete
+        bool ok = true;
+        for (int i = lane; i <= NR; i += 32) ok = ok && h.lock(i, 0, L, i == 0 ? kSiteLockPartial : kSiteLockRoot);
+        ok = __all_sync(0xffffffffu, ok);
+        if (lane == 0) {
+            oc->engaged = ok;
+            if (ok) {
+                const bool pbLoad = H::kHasPartialBuffer && oc->ps != 0;
+                detail::mbar_arrive_expect_tx(&oc->sbar, (NR + (pbLoad ? 1u : 0u)) * nb);
+                for (int i = 1; i <= NR; ++i) h.load(slot(i - 1), i, &oc->sbar);
+                if (pbLoad) h.load(slot(sP), 0, &oc->sbar);
+                unsigned long long t0 = 0;
+                for (unsigned it = 0; !detail::mbar_try_wait(&oc->sbar, 0); ++it)
+                    if (!h.keep_waiting(t0, it, kSiteBulkCopy, -1, 0)) { oc->engaged = 0; break; }
+            }
+        }
+    }
+    __syncthreads();
+    if (!oc->engaged) {
+        // not deep enough (or a failed wait, which left the heap's error
+        // raised): no lend will come; k_delete does the work
+        if (tid == 0) {
+            mb->total = 0;
+            ow::stg_rel(&mb->done, 1);
+        }
+        return;
+    }
+
+    if (warp < kOwnerWarps) {
+        // ================================================= compute warps
+        const int ct = tid;
+        const int wpm = 2 * B / S;  // windows per merge
+        long long dc = oc->dc0;
+        const int lim = oc->lim;
+        const int ps = oc->ps;
+        unsigned long long st[kStCount] = {};
+        const long long tLoop = clock64();
+        for (int d = 0;; ++d) {
+            const int b = d & 1;
+            K* C = slot(sC + b);
+            if (ct == 0) {
+                int stop = 0;
+                if (detail::ld_relaxed(&h.state->err) != 0 || dc + B > lim) {
+                    stop = 1;
+                } else {
+                    const long long tw = clock64();
+                    unsigned long long t0 = 0;
+                    for (unsigned it = 0;; ++it) {
+                        if (ow::lds_acq(&oc->cReady[b]) == d + 1) break;
+                        if (ow::lds_acq(&oc->cEnd) == d) { stop = 1; break; }
+                        if (!h.keep_waiting(t0, it, kSiteLockLast, -1, d)) { stop = 1; break; }
+                    }
+                    st[kStWaitCarried] += clock64() - tw;
+                }
+                // the next delete's last node may be taken during this one
+                if (!stop && dc + 2 * B <= lim) ow::sts_rel(&oc->takeAllowed, d + 2);
+                oc->plStop = stop;
+            }
+            ow::bar_compute();
+            if (oc->plStop) break;
+
+            // refill: the last node merged with the partial buffer (:404-416)
+            if (H::kHasPartialBuffer && ps != 0) {
+                K m[IPT];
+                const bool act = warp < wpm;
+                if (act) ow::window<K, IPT>(C, slot(sP), B, warp * S, m);
+                ow::bar_compute();
+                if (act) ow::window_store<K, IPT>(C, slot(sP), B, warp * S, m);
+                ow::bar_compute();
+            }
+            // deleteRoot's output (:328-329): the root's keys, before the pass rewrites node 1
+            {
+                K* dst = out + dc;
+                const K* src = slot(0);
+                if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+                    const int nv = static_cast<int>(nb / 16);
+                    for (int q = ct; q < nv; q += kOwnerWarps * 32)
+                        reinterpret_cast<uint4*>(dst)[q] = reinterpret_cast<const uint4*>(src)[q];
+                } else {
+                    for (int q = ct; q < B; q += kOwnerWarps * 32) dst[q] = src[q];
+                }
+            }
+            int cur = 1;
+            int lendNode = 0;
+            for (;;) {
+                long long tPass = 0;
+                if (ct == 0) {
+                    const long long tPlan = clock64();
+                    long long tWait = 0;
+                    // plan: follow the smaller child while the carried batch
+                    // starts at or above one child's last key (the fast case
+                    // of the sift, where the node takes the children's lower
+                    // half and the carried batch goes on unchanged)
+                    int nm = 0, gen = 0, node = cur, lev = ow::level_of(cur);
+                    const K c0 = C[0];
+                    while (lev < R) {
+                        const int l = H::leftOf(node), r = H::rightOf(l);
+                        if (lev + 1 == R) {
+                            // a lent child must be back in its slot first
+                            const long long tw = clock64();
+                            for (int k = 0; k < 2; ++k) {
+                                const int x = k ? r : l;
+                                unsigned long long t0 = 0;
+                                for (unsigned it = 0; ow::lds_acq(&oc->lentState[x - firstR]) != 0; ++it)
+                                    if (!h.keep_waiting(t0, it, kSiteLockChild, x, 1)) break;
+                            }
+                            tWait += clock64() - tw;
+                        }
+                        const K* X = slot(l - 1);
+                        const K* Y = slot(r - 1);
+                        const K xl = X[B - 1], yl = Y[B - 1];
+                        // the larger child: heap/tditdd_np/heap.cuh:416 tie rule
+                        const int larger = (xl < yl || (xl == yl && !(xl < h.init_limits) && X[0] < Y[0])) ? r : l;
+                        const int smaller = larger == r ? l : r;
+                        if (c0 < (xl < yl ? xl : yl)) {
+                            gen = node;
+                            oc->genL = l;
+                            oc->genR = r;
+                            oc->genLarger = larger;
+                            oc->genSmaller = smaller;
+                            break;
+                        }
+                        oc->mA[nm] = l - 1;
+                        oc->mB[nm] = r - 1;
+                        oc->mLo[nm] = node - 1;
+                        oc->mHi[nm] = larger - 1;
+                        ++nm;
+                        node = smaller;
+                        ++lev;
+                    }
+                    oc->nm = nm;
+                    oc->gen = gen;
+                    oc->lend = (!gen && lev == R) ? node : 0;
+                    if (oc->lend) {
+                        // post the lend now: the worker's first step needs
+                        // nothing from this pass
+                        const long long tw = clock64();
+                        unsigned long long t0 = 0;
+                        for (unsigned it = 0; oc->lendReq - ow::lds_acq(&oc->lendDone) >= 4; ++it)
+                            if (!h.keep_waiting(t0, it, kSiteHandOff, -1, 0)) break;
+                        st[kStWaitRing] += clock64() - tw;
+                        ow::post_lend(oc, oc->lend, b);
+                        ++st[kStLends];
+                    }
+                    tPass = clock64();
+                    st[kStWaitLent] += tWait;
+                    st[kStPlan] += tPass - tPlan - tWait;
+                    st[kStGeneral] += gen != 0;
+                }
+                ow::bar_compute();
+                const int nm = oc->nm, gen = oc->gen;
+                if (oc->lend) lendNode = oc->lend;
+                // the pass: every planned level's children merge at once
+                {
+                    K m[IPT];
+                    const int q = warp / wpm;
+                    const bool act = q < nm;
+                    if (act) ow::window<K, IPT>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, m);
+                    ow::bar_compute();
+                    if (act) ow::window_store<K, IPT>(slot(oc->mLo[q]), slot(oc->mHi[q]), B, (warp - q * wpm) * S, m);
+                    ow::bar_compute();
+                }
+                if (!gen) {
+                    if (ct == 0) st[kStPass] += clock64() - tPass;
+                    break;
+                }
+                // the general sift step at node `gen` (heap/tditdd/heap.cuh:
+                // 418-532): children merge, lower half to T, upper half to the
+                // larger child, then the case analysis against the carried batch
+                {
+                    K m[IPT];
+                    const bool act = warp < wpm;
+                    if (act) ow::window<K, IPT>(slot(oc->genL - 1), slot(oc->genR - 1), B, warp * S, m);
+                    ow::bar_compute();
+                    if (act) ow::window_store<K, IPT>(slot(sT), slot(oc->genLarger - 1), B, warp * S, m);
+                    ow::bar_compute();
+                }
+                if (ct == 0) {
+                    const K* T = slot(sT);
+                    int sel;
+                    if (!(C[0] < T[B - 1])) sel = 0;  // node takes T, the carried batch goes on
+                    else if (H::kVariant == kTopDown || !H::kHasPartialBuffer ? (C[B - 1] <= T[0]) : (C[B - 1] < T[0]))
+                        sel = 1;  // node takes C, the smaller child takes T: done (buitdd alone uses <, :451)
+                    else sel = 2;  // merge C with T: lower to the node, upper carried on
+                    oc->caseSel = sel;
+                }
+                ow::bar_compute();
+                const int sel = oc->caseSel;
+                const int g = gen, sm = oc->genSmaller;
+                if (sel == 0) {
+                    for (int q = ct; q < B; q += kOwnerWarps * 32) slot(g - 1)[q] = slot(sT)[q];
+                } else if (sel == 1) {
+                    for (int q = ct; q < B; q += kOwnerWarps * 32) {
+                        slot(g - 1)[q] = C[q];
+                        slot(sm - 1)[q] = slot(sT)[q];
+                    }
+                } else {
+                    K m[IPT];
+                    const bool act = warp < wpm;
+                    if (act) ow::window<K, IPT>(C, slot(sT), B, warp * S, m);
+                    ow::bar_compute();
+                    if (act) ow::window_store<K, IPT>(slot(g - 1), C, B, warp * S, m);
+                }
+                ow::bar_compute();
+                if (ct == 0) st[kStPass] += clock64() - tPass;
+                if (sel == 1) break;
+                cur = sm;
+                if (ow::level_of(cur) == R) {
+                    // the sift goes on below the resident levels: lend cur
+                    // with the (possibly changed) carried batch
+                    if (ct == 0) {
+                        const long long tw = clock64();
+                        unsigned long long t0 = 0;
+                        for (unsigned it = 0; oc->lendReq - ow::lds_acq(&oc->lendDone) >= 4; ++it)
+                            if (!h.keep_waiting(t0, it, kSiteHandOff, -1, 0)) break;
+                        st[kStWaitRing] += clock64() - tw;
+                        ow::post_lend(oc, cur, b);
+                        ++st[kStLends];
+                    }
+                    lendNode = cur;
+                    break;
+                }
+            }
+            if (ct == 0) {
+                // the lent node's slot was read by this delete's pass: only now
+                // may the returner reload it
+                if (lendNode) ow::sts_rel(&oc->lentState[lendNode - firstR], 1);
+                else atomicAdd(&oc->cFree[b], 1);  // no lend: the buffer is free again
+            }
+            dc += B;
+        }
+        if (ct == 0) {
+            h.state->deleteCount = static_cast<int>(dc);
+            st[kStDeletes] = static_cast<unsigned long long>((dc - oc->dc0) / B);
+            st[kStLoop] = clock64() - tLoop;
+            for (int i = 0; i < 8; ++i) mb->stats[i] = st[i];
+            mb->stats[kStLends] = st[kStLends];
+            ow::sts_rel(&oc->stop, 1);
+        }
+    } else if (warp == kOwnerWarps) {
+        // ================================================= taker
+        int bc = oc->bc0;
+        unsigned long long tkLock = 0, tkLoad = 0, tkIdle = 0;
+        for (int t = 0;; ++t) {
+            const int b = t & 1;
+            int go = 0;
+            if (lane == 0) {
+                const long long ti = clock64();
+                unsigned long long t0 = 0;
+                for (unsigned it = 0;; ++it) {
+                    if (ow::lds_acq(&oc->stop)) break;
+                    if (ow::lds_acq(&oc->takeAllowed) > t && ow::lds_acq(&oc->cFree[b]) >= (t >> 1)) { go = 1; break; }
+                    if (!h.keep_waiting(t0, it, kSiteLockLast, -1, t)) break;
+                    __nanosleep(32);
+                }
+                tkIdle += clock64() - ti;
+                if (go && bc < (2 << R)) {  // the last node would be resident: the owner is done
+                    ow::sts_rel(&oc->cEnd, t);
+                    go = 0;
+                }
+                if (go) {
+                    // deleteUpdate takes the last node (:355-402): lock it
+                    const long long tl = clock64();
+                    bool ok;
+                    if constexpr (H::kVariant == kTopDown) {
+                        ok = h.lock(bc, TD::AVAIL, TD::INUSE, kSiteLockLast);
+                    } else {
+                        ok = true;
+                        unsigned long long t1 = 0;
+                        for (unsigned it = 0; detail::max_acquire(h.status + bc, BU::INUSE) == BU::INUSE; ++it)
+                            if (!h.keep_waiting(t1, it, kSiteLockLast, bc, BU::INUSE)) { ok = false; break; }
+                    }
+                    const long long tb = clock64();
+                    tkLock += tb - tl;
+                    if (ok) {
+                        detail::fence_proxy_async_smem();
+                        detail::mbar_arrive_expect_tx(&oc->cbar[b], nb);
+                        h.load(slot(sC + b), bc, &oc->cbar[b]);
+                        unsigned long long t1 = 0;
+                        for (unsigned it = 0; !detail::mbar_try_wait(&oc->cbar[b], (t >> 1) & 1); ++it)
+                            if (!h.keep_waiting(t1, it, kSiteBulkCopy, bc, 0)) { ok = false; break; }
+                    }
+                    tkLoad += clock64() - tb;
+                    if (ok) ow::sts_rel(&oc->cReady[b], t + 1);
+                    else ow::sts_rel(&oc->cEnd, t);
+                    go = ok ? 2 : 0;
+                }
+            }
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (go != 2) break;
+            // reset the taken node (:396) and release it
+            {
+                K* g = h.node(bc);
+                const int nv = static_cast<int>(nb / 16);
+                const uint4 pat = detail::splat16<K>(h.init_limits);
+                for (int q = lane; q < nv; q += 32) reinterpret_cast<uint4*>(g)[q] = pat;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                H::fence();
+                h.setState(bc, 0);
+            }
+            --bc;
+        }
+        if (lane == 0) {
+            oc->bcFinal = bc;
+            mb->stats[kStTakeLock] = tkLock;
+            mb->stats[kStTakeLoad] = tkLoad;
+            mb->stats[kStTakeIdle] = tkIdle;
+        }
+    } else if (warp == kOwnerWarps + 1) {
+        // ================================================= lender
+        for (int q = 0;; ++q) {
+            int go = 0;
+            if (lane == 0) {
+                unsigned long long t0 = 0;
+                for (unsigned it = 0;; ++it) {
+                    if (ow::lds_acq(&oc->lendReq) > q) { go = 1; break; }
+                    if (ow::lds_acq(&oc->stop) && ow::lds_acq(&oc->lendReq) <= q) break;
+                    if (!h.keep_waiting(t0, it, kSiteHandOff, -1, q)) break;
+                    __nanosleep(32);
+                }
+                if (go) {
+                    // the entry's previous lend must have been read by its worker
+                    const int e = q % kMboxEntries;
+                    unsigned long long t1 = 0;
+                    for (unsigned it = 0; detail::ld_acquire(&mb->cons[e]) != q / kMboxEntries; ++it)
+                        if (!h.keep_waiting(t1, it, kSiteHandOff, -1, q)) { go = 0; break; }
+                }
+            }
+            go = __shfl_sync(0xffffffffu, go, 0);
+            if (!go) {
+                if (lane == 0) {
+                    mb->total = q;
+                    ow::stg_rel(&mb->done, 1);
+                }
+                break;
+            }
+            const int e = q % kMboxEntries;
+            const int b = oc->reqBuf[q & 3];
+            {
+                const uint4* src = reinterpret_cast<const uint4*>(slot(sC + b));
+                uint4* dst = reinterpret_cast<uint4*>(mdata + static_cast<size_t>(e) * B);
+                const int nv = static_cast<int>(nb / 16);
+                for (int v = lane; v < nv; v += 32) dst[v] = src[v];
+            }
+            __syncwarp();
+            if (lane == 0) {
+                mb->node[e] = oc->reqNode[q & 3];
+                H::fence();
+                ow::stg_rel(&mb->seq[e], q + 1);
+                atomicAdd(&oc->cFree[b], 1);
+                ow::sts_rel(&oc->lendDone, q + 1);
+            }
+        }
+    } else {
+        // ================================================= returner
+        // lane i watches level-R node 2^R + i while it is lent
+        const int nR = 1 << R;
+        unsigned phase = 0, reloads = 0;
+        unsigned long long t0 = 0;
+        unsigned it = 0;
+        for (;;) {
+            // `stop` first: the compute warps mark their last lend before they
+            // set it, so a scan that follows a seen `stop` finds every lend
+            const int stop = __shfl_sync(0xffffffffu, lane == 0 ? ow::lds_acq(&oc->stop) : 0, 0);
+            int st = 0;
+            if (lane < nR) {
+                st = ow::lds_acq(&oc->lentState[lane]);
+                if (st == 1) {
+                    const int x = firstR + lane;
+                    if (detail::ld_relaxed(h.status + x) == 0 && detail::cas_acquire(h.status + x, 0, L) == 0) {
+                        detail::fence_proxy_async_smem();
+                        detail::mbar_arrive_expect_tx(&oc->rbar[lane], nb);
+                        h.load(slot(x - 1), x, &oc->rbar[lane]);
+                        unsigned long long t1 = 0;
+                        bool ok = true;
+                        for (unsigned i2 = 0; !detail::mbar_try_wait(&oc->rbar[lane], phase); ++i2)
+                            if (!h.keep_waiting(t1, i2, kSiteBulkCopy, x, 0)) { ok = false; break; }
+                        phase ^= 1u;
+                        ++reloads;
+                        st = ok ? 0 : 2;
+                        ow::sts_rel(&oc->lentState[lane], st);
+                        t0 = 0;
+                        it = 0;
+                    } else if (!h.keep_waiting(t0, it++, kSiteLockChild, x, 0)) {
+                        st = 2;
+                        ow::sts_rel(&oc->lentState[lane], st);
+                    }
+                }
+            }
+            const bool pending = __any_sync(0xffffffffu, st == 1);
+            if (stop && !pending) {
+                for (int o = 16; o > 0; o >>= 1) reloads += __shfl_xor_sync(0xffffffffu, reloads, o);
+                if (lane == 0) mb->stats[kStReloads] = reloads;
+                break;
+            }
+            __nanosleep(pending ? 32 : 128);
+        }
+    }
+    __syncthreads();
+
+    // ---- write-back: resident nodes and the partial buffer to their global
+    // nodes, counters, then every lock word released
+    {
+        const int nv = static_cast<int>(nb / 16);
+        for (int i = 1; i <= NR; ++i) {
+            const uint4* src = reinterpret_cast<const uint4*>(slot(i - 1));
+            uint4* dst = reinterpret_cast<uint4*>(h.node(i));
+            for (int v = tid; v < nv; v += blockDim.x) dst[v] = src[v];
+        }
+        if (H::kHasPartialBuffer && oc->ps != 0) {
+            const uint4* src = reinterpret_cast<const uint4*>(slot(sP));
+            uint4* dst = reinterpret_cast<uint4*>(h.node(0));
+            for (int v = tid; v < nv; v += blockDim.x) dst[v] = src[v];
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        h.state->batchCount = oc->bcFinal;
+        H::fence();
+        for (int i = 0; i <= NR; ++i) h.setState(i, 0);
+        detail::mbar_inval(&oc->cbar[0]);
+        detail::mbar_inval(&oc->cbar[1]);
+        detail::mbar_inval(&oc->sbar);
+        for (int i = 0; i < (1 << kOwnerMaxR); ++i) detail::mbar_inval(&oc->rbar[i]);
+    }
+}
+
+// Block 0 owns the top of the heap, the rest are workers.  blockDim.x must
+// be 1024 (29 compute warps and 3 control warps in the owner).
+template <typename H, typename K>
+__global__ void __launch_bounds__(1024) k_delete_owner(H h, K* out, Mailbox* mb, K* mdata, int R) {
+    if (blockIdx.x == 0) owner_block<H, K>(h, out, mb, mdata, R);
+    else owner_worker<H, K>(h, mb, mdata);
+}
+
+}  // namespace impl
+}  // namespace gh

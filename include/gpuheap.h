@@ -64,7 +64,12 @@ gh_status gh_heap_set_grid(gh_heap* h, int blocks);
 
 /* insertKernel (test/heap_test.cu:44-58, artifacts/synthetic/sort.cu:32-46):
  * inserts keys_dev[0, n) in insertion() calls of `chunk` keys (0 = batch_size;
- * chunk <= batch_size), spread over the heap's grid. */
+ * chunk <= batch_size), spread over the heap's grid.  With chunk = batch_size
+ * and the partial buffer empty, the full batches' target nodes are reserved
+ * in one step before they are inserted, so they do not take node 0 one at a
+ * time; the result is a heap that the same inserts could have built one by
+ * one.  No other operation may use the heap during the call (the reference's
+ * tests run insertKernel as a phase of its own). */
 gh_status gh_heap_insert(gh_heap* h, const void* keys_dev, long long n, int chunk, void* stream);
 
 /* deleteKernel (test/heap_test.cu:60-77): deleteRoot/deleteUpdate until the
@@ -362,6 +367,18 @@ gh_status gh_gen_grid(int width, int height, unsigned long long seed, int obstac
 
 /* Number of kernels this library has launched since it was loaded. */
 long long gh_launch_count(void);
+
+/* Counters of the last owner-mode bulk delete on this heap (gh_heap_delete
+ * and gh_heap_sort run one when the heap is deep enough; it has no
+ * counterpart in the reference, whose deleteKernel is the plain loop).  Up to
+ * n of: [0] deletes made by the owner block, SM cycles of its delete loop
+ * spent [1] waiting for the next last node, [2] waiting for a lent node to
+ * come back, [3] waiting for room to lend, [4] planning paths, [5] merging;
+ * [6] general sift steps; [7] cycles of the whole loop; the last-node taker's
+ * cycles [8] in lock waits, [9] in bulk loads, [10] idle; [11] lends;
+ * [12] lent nodes taken back.  Synchronizes the device.  All zero when the
+ * heap has no owner mode (batch_size below 512) or none has run. */
+gh_status gh_heap_owner_stats(gh_heap* h, unsigned long long* out, int n);
 
 /* Properties. */
 gh_status gh_heap_info(gh_heap* h, int* key_kind, int* variant, int* partial_buffer, int* batch_num,

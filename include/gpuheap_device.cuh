@@ -80,7 +80,10 @@ struct alignas(128) HeapState {
     int pad1[28];
     int busy;               // applications: blocks between taking a batch and finishing its inserts
     int insTicket;          // bottom-up inserts: next park ticket (atomicAdd)
-    int pad2[14];
+    int resvBase;           // bulk insert: targets resvBase+1 .. resvBase+resvCount are reserved
+    int resvCount;          // 0: no reservation (the bulk insert takes node 0 per batch)
+    int resvTurn;           // top-down reserved inserts take the root in target order: the next target
+    int pad2[11];
     unsigned long long appStats[8];  // applications: counters (e.g. pops, expansions, relaxations)
 };
 
@@ -108,6 +111,11 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 __device__ __forceinline__ int ld_relaxed(const int* p) {
     int v;
     asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
 __device__ __forceinline__ void st_relaxed(int* p, int v) {
@@ -332,6 +340,7 @@ struct Heap {
     // batch), the partial buffer (or loaded node) and the two children.
     static constexpr int kBufs = 4;
     static constexpr bool kHasPartialBuffer = PB;
+    static constexpr int kVariant = VARIANT;
     static __host__ __device__ size_t smemBytes(int bs) {
         return kBufs * static_cast<size_t>(bs) * sizeof(K) + sizeof(OpCtl) + 16;
     }
@@ -659,27 +668,67 @@ struct Heap {
         else insert_bottomup(op, s0, s1, s2, bc, parkTag);
     }
 
+    // Insertion of one full batch into `target`, a node that a bulk driver
+    // reserved before any of its inserts began: batchCount already counts
+    // it and its lock word already holds the state the insert would have
+    // claimed (TARGET top-down, INUSE bottom-up).  With the partial buffer
+    // empty and the batch full, the reference's insertion changes node 0
+    // not at all (case 2.2 with ps = 0 merges against padding) and holds it
+    // only to draw the target, so this form takes no node-0 lock: the
+    // bulk inserts pass the top of the heap without a serial hand-off.
+    // Every other step is insertion()'s.  Callers: the bulk insert driver
+    // only, with no deleter on the heap during its launch.
+    __device__ __forceinline__ void insertionReserved(const K* items, int target, int smemOffset) const {
+        K* s0 = region(smemOffset);
+        K* s1 = s0 + batchSize;
+        K* s2 = s1 + batchSize;
+        Op op(this, ctl(s0));
+        const int B = batchSize;
+        const int tid = threadIdx.x;
+        int parkTag = 0;
+        if constexpr (VARIANT == kBottomUp) {
+            if (tid == 0) parkTag = BU::kParkBase + (atomicAdd(&state->insTicket, 1) & BU::kTicketMask);
+        }
+        for (int q = tid; q < B; q += blockDim.x) s0[q] = items[q];
+        __syncthreads();
+        detail::bitonic_sort(s0, B);
+        if constexpr (VARIANT == kTopDown) insert_topdown(op, s0, s1, s2, target - 1, true);
+        else insert_bottomup(op, s0, s1, s2, target - 1, parkTag, true);
+    }
+
     // Top-down path (heap/tditdd/heap.cuh:666-752).  Entered holding node 0;
     // the carried batch is in s0.  Each node on the root -> target path is
     // held while its merge runs; the next node is locked and its load started
     // before this one is released (locking it before the merge measured
     // slower: it lengthens the hold).
-    __device__ __forceinline__ void insert_topdown(Op& op, K* s0, K* s1, K* s2, int bc) const {
+    // `reserved`: the target (bc + 1) was reserved by a bulk driver
+    // (insertionReserved): no capacity check, counter update, target claim
+    // or node-0 release here.
+    __device__ __forceinline__ void insert_topdown(Op& op, K* s0, K* s1, K* s2, int bc, bool reserved = false) const {
         OpCtl* c = op.c;
         const int tid = threadIdx.x;
         if (tid == 0) {
             const int target = bc + 1;
-            bool ok = target <= batchNum;
-            if (!ok) raise(kErrCapacity, kSiteCapacity, target, 0);
-            if (ok) detail::st_relaxed(&state->batchCount, target);
-            ok = ok && lock(target, TD::AVAIL, TD::TARGET, kSiteLockTarget);
+            bool ok = true;
+            if (!reserved) {
+                ok = target <= batchNum;
+                if (!ok) raise(kErrCapacity, kSiteCapacity, target, 0);
+                if (ok) detail::st_relaxed(&state->batchCount, target);
+                ok = ok && lock(target, TD::AVAIL, TD::TARGET, kSiteLockTarget);
+            }
+            if (ok && reserved) ok = waitTurn(target);
             if (ok && target != 1) {
                 ok = lock(1, TD::AVAIL, TD::INUSE, kSiteLockRoot);
                 if (ok) { op.issue(nodeBytes()); load(s1, 1, &c->bar); }
             }
+            // reserved inserts enter the root in target order, as the
+            // reference's do by claiming targets under the node-0 lock: a
+            // later target's walk waits at an earlier one's (an ancestor's)
+            // TARGET word, so the earlier insert must never queue behind it
+            if (ok && reserved) detail::st_release(&state->resvTurn, target + 1);
             // the root is ours: release the partial buffer (the reference does
             // this at the top of the first path step, :692-694)
-            if (ok) unlock(0, TD::AVAIL);
+            if (ok && !reserved) unlock(0, TD::AVAIL);
             c->abort = !ok;
             c->w[0] = target;
         }
@@ -761,17 +810,21 @@ struct Heap {
     // it wrote, which can leave them below the grandparent, and only this walk
     // repairs that.  Stopping early in that case left parent/grandparent
     // inversions behind when inserts and deletes ran concurrently.
-    __device__ __forceinline__ void insert_bottomup(Op& op, K* s0, K* s1, K* s2, int bc, int parkTag) const {
+    __device__ __forceinline__ void insert_bottomup(Op& op, K* s0, K* s1, K* s2, int bc, int parkTag,
+                                                    bool reserved = false) const {
         OpCtl* c = op.c;
         const int tid = threadIdx.x;
         const int B = batchSize;
         if (tid == 0) {
             const int target = bc + 1;
-            bool ok = target <= batchNum;
-            if (!ok) raise(kErrCapacity, kSiteCapacity, target, 0);
-            if (ok) detail::st_relaxed(&state->batchCount, target);
-            ok = ok && lock(target, BU::AVAIL, BU::INUSE, kSiteLockTarget);
-            if (ok) unlock(0, BU::AVAIL);
+            bool ok = true;
+            if (!reserved) {
+                ok = target <= batchNum;
+                if (!ok) raise(kErrCapacity, kSiteCapacity, target, 0);
+                if (ok) detail::st_relaxed(&state->batchCount, target);
+                ok = ok && lock(target, BU::AVAIL, BU::INUSE, kSiteLockTarget);
+                if (ok) unlock(0, BU::AVAIL);
+            }
             c->abort = !ok;
             c->w[0] = target;
         }
@@ -835,6 +888,14 @@ struct Heap {
             cur = p;
         }
         if (tid == 0) unlock(1, BU::AVAIL);  // (:685-688)
+    }
+
+    // Thread 0: waits (bounded) until the reserved-insert turn reaches `target`.
+    __device__ __forceinline__ bool waitTurn(int target) const {
+        unsigned long long t0 = 0;
+        for (unsigned it = 0; detail::ld_acquire(&state->resvTurn) != target; ++it)
+            if (!keep_waiting(t0, it, kSiteLockRoot, 1, detail::ld_relaxed(&state->resvTurn))) return false;
+        return true;
     }
 
     // ------------------------------------------------------------------ deleteRoot
