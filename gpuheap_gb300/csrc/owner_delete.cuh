@@ -14,7 +14,8 @@
 //   * a delete's sift steps at levels 0..R-1 only read the children's last
 //     keys to pick the path and only merge children into their parent, so
 //     once the path is known they are independent: the owner plans the
-//     path (one thread), then merges every level of it at once (29 warps);
+//     path (one warp), then merges every level of it at once (one warp per
+//     window of the merges);
 //   * the sift continues below level R in a worker block (every other block
 //     of the launch): the owner lends it the level-R node on the path
 //     together with the carried batch through a mailbox in global memory,
@@ -43,8 +44,12 @@ namespace impl {
 
 constexpr int kMboxEntries = 32;   // lends in flight between owner and workers
 constexpr int kOwnerWarps = 29;    // compute warps of the owner block
-constexpr int kOwnerIpt = 16;      // keys per lane of a merge window (window = 512 keys)
 constexpr int kOwnerMaxR = 4;      // deepest resident level
+
+// Keys per lane of a merge window: 32 for 4-byte keys (a window of 1024
+// keys, sorted with two shared-memory transposes), 16 for 8-byte keys (512,
+// sorted with lane shuffles; 32 would not fit the registers).
+__host__ __device__ constexpr int owner_ipt(int keyBytes) { return keyBytes == 8 ? 16 : 32; }
 
 // Mailbox in global memory: lend q (q = 0, 1, ...) sits in entry q % 32 with
 // its carried batch at data + entry * batchSize.
@@ -80,6 +85,7 @@ enum OwnerStat : int {
 
 // Shared-memory control words of the owner block (after its node slots).
 struct alignas(16) OwnerCtl {
+    unsigned long long st[16];                  // counters (OwnerStat), compute thread 0
     unsigned long long cbar[2];                 // bulk loads of the two carried-batch buffers
     unsigned long long rbar[1 << kOwnerMaxR];   // bulk reloads of lent level-R nodes
     unsigned long long sbar;                    // set-up loads
@@ -101,24 +107,29 @@ struct alignas(16) OwnerCtl {
     int caseSel;
 };
 
+// Transpose scratch of one merge window (32 x 33 keys, one pad column).
+inline size_t owner_scratch(int keyBytes) { return owner_ipt(keyBytes) == 32 ? 32 * 33 * keyBytes : 0; }
+// Shared memory of the owner block: 2^(R+1) + 3 node slots, the merge
+// windows' scratch, the control words.
+inline size_t owner_smem(int batchSize, int keyBytes, int R) {
+    const int windows = R * (2 * batchSize / (32 * owner_ipt(keyBytes)));
+    return static_cast<size_t>((2 << R) + 3) * batchSize * keyBytes + windows * owner_scratch(keyBytes) +
+           sizeof(OwnerCtl);
+}
 // Resident depth R for a batch size and key size (0: no owner mode): the
-// deepest R <= 4 whose 2^(R+1) + 3 node slots fit in 200 KB of shared memory
-// and whose R merges fit the compute warps.
+// deepest R <= 4 whose shared memory fits in 216 KB and whose R merges fit
+// the compute warps (one window per warp).
 inline int owner_depth(int batchSize, int keyBytes) {
     if (batchSize < 512 || 2 * batchSize / 1024 > 8) return 0;
     for (int R = kOwnerMaxR; R >= 2; --R) {
-        const size_t bytes = static_cast<size_t>((2 << R) + 3) * batchSize * keyBytes + sizeof(OwnerCtl);
-        const int windows = R * (2 * batchSize / (32 * kOwnerIpt));
-        if (bytes <= 200 * 1024 && windows <= kOwnerWarps) return R;
+        const int windows = R * (2 * batchSize / (32 * owner_ipt(keyBytes)));
+        if (owner_smem(batchSize, keyBytes, R) <= 216 * 1024 && windows <= kOwnerWarps && windows >= R) return R;
     }
     return 0;
 }
 // Bytes of the mailbox and its lend buffers for a heap.
 inline size_t mbox_bytes(int batchSize, int keyBytes) {
     return sizeof(Mailbox) + static_cast<size_t>(kMboxEntries) * batchSize * keyBytes;
-}
-inline size_t owner_smem(int batchSize, int keyBytes, int R) {
-    return static_cast<size_t>((2 << R) + 3) * batchSize * keyBytes + sizeof(OwnerCtl);
 }
 
 namespace ow {
@@ -172,7 +183,29 @@ __device__ __forceinline__ int warp_split(const K* a, const K* b, int n, int D) 
 // bitonic sequence, sorted by a bitonic network (strides >= 32 inside the
 // registers, < 32 across lanes).  Reads only shared memory.
 template <typename K, int IPT>
-__device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (&m)[IPT]) {
+__device__ __forceinline__ void sort_regs(K (&m)[IPT]) {
+#pragma unroll
+    for (int s = IPT / 2; s > 0; s >>= 1) {
+#pragma unroll
+        for (int r = 0; r < IPT; ++r)
+            if ((r & s) == 0) {
+                const K u = m[r], v = m[r + s];
+                m[r] = u < v ? u : v;
+                m[r + s] = u < v ? v : u;
+            }
+    }
+}
+
+// One merge window: outputs [D, D + 32*IPT) of merge(a, b) into m, element
+// k = r*32 + lane in m[r].  The window's keys are the 32*IPT smallest of
+// a[i0, i0+S) and b[j0, j0+S): min(x_k, y_{S-1-k}) is that set as a
+// bitonic sequence, sorted by a bitonic network.  Strides >= 32 compare
+// keys inside a lane's registers; for strides < 32, IPT = 32 transposes the
+// window through `scr` (32 x 33 keys of this warp: both access patterns hit
+// 32 different banks) so that they are inside the registers too, and back;
+// IPT = 16 uses lane shuffles.  Reads shared memory only.
+template <typename K, int IPT>
+__device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (&m)[IPT], K* scr) {
     constexpr int S = 32 * IPT;
     const int lane = threadIdx.x & 31;
     const int i0 = warp_split(a, b, n, D), j0 = D - i0;
@@ -185,34 +218,41 @@ __device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (
         const K y = yi < n ? b[yi] : top;
         m[r] = x < y ? x : y;
     }
+    sort_regs<K, IPT>(m);
+    if constexpr (IPT == 32) {
+        // the sorted window stays in scr (element k at (k/32)*33 + k%32)
+        // for window_store: nothing is held in registers across the barrier
 #pragma unroll
-    for (int s = IPT / 2; s > 0; s >>= 1) {
+        for (int r = 0; r < 32; ++r) scr[r * 33 + lane] = m[r];
+        __syncwarp();
 #pragma unroll
-        for (int r = 0; r < IPT; ++r)
-            if ((r & s) == 0) {
-                const K u = m[r], v = m[r + s];
-                m[r] = u < v ? u : v;
-                m[r + s] = u < v ? v : u;
+        for (int q = 0; q < 32; ++q) m[q] = scr[lane * 33 + q];
+        sort_regs<K, IPT>(m);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) scr[lane * 33 + q] = m[q];
+    } else {
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) {
+            const bool upper = (lane & s) != 0;
+#pragma unroll
+            for (int r = 0; r < IPT; ++r) {
+                const K o = __shfl_xor_sync(0xffffffffu, m[r], s);
+                m[r] = upper ? (m[r] > o ? m[r] : o) : (m[r] < o ? m[r] : o);
             }
-    }
-#pragma unroll
-    for (int s = 16; s > 0; s >>= 1) {
-        const bool upper = (lane & s) != 0;
-#pragma unroll
-        for (int r = 0; r < IPT; ++r) {
-            const K o = __shfl_xor_sync(0xffffffffu, m[r], s);
-            m[r] = upper ? (m[r] > o ? m[r] : o) : (m[r] < o ? m[r] : o);
         }
     }
 }
+// Writes the window's outputs to lo[0, n) / hi[0, n) (from scr when IPT = 32).
 template <typename K, int IPT>
-__device__ __forceinline__ void window_store(K* lo, K* hi, int n, int D, const K (&m)[IPT]) {
+__device__ __forceinline__ void window_store(K* lo, K* hi, int n, int D, const K (&m)[IPT], const K* scr) {
     const int lane = threadIdx.x & 31;
+    if constexpr (IPT == 32) __syncwarp();
 #pragma unroll
     for (int r = 0; r < IPT; ++r) {
         const int o = D + r * 32 + lane;
-        if (o < n) lo[o] = m[r];
-        else hi[o - n] = m[r];
+        const K v = IPT == 32 ? scr[r * 33 + lane] : m[r];
+        if (o < n) lo[o] = v;
+        else hi[o - n] = v;
     }
 }
 
@@ -271,16 +311,20 @@ __device__ void owner_worker(const H& h, Mailbox* mb, const K* mdata) {
 template <typename H, typename K>
 __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
     extern __shared__ __align__(16) unsigned char gh_dyn_smem[];
-    constexpr int IPT = kOwnerIpt;
+    constexpr int IPT = owner_ipt(sizeof(K));
     constexpr int S = 32 * IPT;
     const int B = h.batchSize;
     const int NR = (2 << R) - 1;       // resident nodes 1..NR; node i in slot i-1
     const int firstR = 1 << R;         // level-R nodes firstR .. NR
     const int sP = NR, sC = NR + 1, sT = NR + 3;
+    const int wpm = 2 * B / S;         // windows per merge
     K* slots = reinterpret_cast<K*>(gh_dyn_smem);
-    OwnerCtl* oc = reinterpret_cast<OwnerCtl*>(slots + static_cast<size_t>(NR + 4) * B);
+    K* scratch = slots + static_cast<size_t>(NR + 4) * B;
+    constexpr int kScr = IPT == 32 ? 32 * 33 : 0;  // keys of one window's scratch
+    OwnerCtl* oc = reinterpret_cast<OwnerCtl*>(scratch + static_cast<size_t>(R * wpm) * kScr);
     auto slot = [&](int s) -> K* { return slots + static_cast<size_t>(s) * B; };
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    K* scr = scratch + static_cast<size_t>(warp < R * wpm ? warp : 0) * kScr;  // this warp's window scratch
     const unsigned nb = h.nodeBytes();
     constexpr int L = H::lockedState();
 
@@ -341,18 +385,22 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
     if (warp < kOwnerWarps) {
         // ================================================= compute warps
         const int ct = tid;
-        const int wpm = 2 * B / S;  // windows per merge
         long long dc = oc->dc0;
         const int lim = oc->lim;
         const int ps = oc->ps;
-        unsigned long long st[kStCount] = {};
+        unsigned long long* st = oc->st;  // in shared memory: thread 0 alone counts
+        if (ct == 0)
+            for (int i = 0; i < kStCount; ++i) st[i] = 0;
         const long long tLoop = clock64();
         for (int d = 0;; ++d) {
             const int b = d & 1;
             K* C = slot(sC + b);
             if (ct == 0) {
                 int stop = 0;
-                if (detail::ld_relaxed(&h.state->err) != 0 || dc + B > lim) {
+                // the heap's error word lives in global memory: a round trip,
+                // so only every 64th delete reads it (the bounded waits below
+                // stop on an error anyway)
+                if (((d & 63) == 63 && detail::ld_relaxed(&h.state->err) != 0) || dc + B > lim) {
                     stop = 1;
                 } else {
                     const long long tw = clock64();
@@ -375,89 +423,121 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
             if (H::kHasPartialBuffer && ps != 0) {
                 K m[IPT];
                 const bool act = warp < wpm;
-                if (act) ow::window<K, IPT>(C, slot(sP), B, warp * S, m);
+                if (act) ow::window<K, IPT>(C, slot(sP), B, warp * S, m, scr);
                 ow::bar_compute();
-                if (act) ow::window_store<K, IPT>(C, slot(sP), B, warp * S, m);
+                if (act) ow::window_store<K, IPT>(C, slot(sP), B, warp * S, m, scr);
                 ow::bar_compute();
             }
-            // deleteRoot's output (:328-329): the root's keys, before the pass rewrites node 1
-            {
+            // deleteRoot's output (:328-329): the root's keys, before the pass
+            // rewrites node 1; warps 1.. copy, so that warp 0, which plans and
+            // signals with release stores, has no global stores in flight
+            if (warp > 0) {
                 K* dst = out + dc;
                 const K* src = slot(0);
+                const int t = ct - 32, nt = (kOwnerWarps - 1) * 32;
                 if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
                     const int nv = static_cast<int>(nb / 16);
-                    for (int q = ct; q < nv; q += kOwnerWarps * 32)
+                    for (int q = t; q < nv; q += nt)
                         reinterpret_cast<uint4*>(dst)[q] = reinterpret_cast<const uint4*>(src)[q];
                 } else {
-                    for (int q = ct; q < B; q += kOwnerWarps * 32) dst[q] = src[q];
+                    for (int q = t; q < B; q += nt) dst[q] = src[q];
                 }
             }
             int cur = 1;
             int lendNode = 0;
             for (;;) {
                 long long tPass = 0;
-                if (ct == 0) {
+                if (warp == 0) {
                     const long long tPlan = clock64();
                     long long tWait = 0;
                     // plan: follow the smaller child while the carried batch
                     // starts at or above one child's last key (the fast case
                     // of the sift, where the node takes the children's lower
-                    // half and the carried batch goes on unchanged)
-                    int nm = 0, gen = 0, node = cur, lev = ow::level_of(cur);
-                    const K c0 = C[0];
-                    while (lev < R) {
-                        const int l = H::leftOf(node), r = H::rightOf(l);
-                        if (lev + 1 == R) {
-                            // a lent child must be back in its slot first
-                            const long long tw = clock64();
-                            for (int k = 0; k < 2; ++k) {
-                                const int x = k ? r : l;
-                                unsigned long long t0 = 0;
-                                for (unsigned it = 0; ow::lds_acq(&oc->lentState[x - firstR]) != 0; ++it)
-                                    if (!h.keep_waiting(t0, it, kSiteLockChild, x, 1)) break;
-                            }
-                            tWait += clock64() - tw;
-                        }
+                    // half and the carried batch goes on unchanged).  Lane i
+                    // first reads the children of resident node i+1 (which is
+                    // larger, by the heap/tditdd_np/heap.cuh:416 tie rule, and
+                    // their smaller last key); the walk then takes one
+                    // shuffle per level.  Children lent out are read on the way.
+                    auto children = [&](int l, int r, int& larger, int& smaller, K& mn) {
                         const K* X = slot(l - 1);
                         const K* Y = slot(r - 1);
                         const K xl = X[B - 1], yl = Y[B - 1];
-                        // the larger child: heap/tditdd_np/heap.cuh:416 tie rule
-                        const int larger = (xl < yl || (xl == yl && !(xl < h.init_limits) && X[0] < Y[0])) ? r : l;
-                        const int smaller = larger == r ? l : r;
-                        if (c0 < (xl < yl ? xl : yl)) {
+                        larger = (xl < yl || (xl == yl && !(xl < h.init_limits) && X[0] < Y[0])) ? r : l;
+                        smaller = larger == r ? l : r;
+                        mn = xl < yl ? xl : yl;
+                    };
+                    int pLarger = 0, pSmaller = 0, pOk = 0;
+                    K pMin = K();
+                    if (lane < firstR - 1) {
+                        const int v = lane + 1, l = H::leftOf(v), r = H::rightOf(l);
+                        pOk = ow::level_of(l) < R ||
+                              (ow::lds_acq(&oc->lentState[l - firstR]) == 0 && ow::lds_acq(&oc->lentState[r - firstR]) == 0);
+                        if (pOk) children(l, r, pLarger, pSmaller, pMin);
+                    }
+                    const K c0 = C[0];
+                    int nm = 0, gen = 0, node = cur, lev = ow::level_of(cur);
+                    while (lev < R) {
+                        const int i = node - 1;
+                        int larger = __shfl_sync(0xffffffffu, pLarger, i);
+                        int smaller = __shfl_sync(0xffffffffu, pSmaller, i);
+                        K mn = __shfl_sync(0xffffffffu, pMin, i);
+                        const int ok = __shfl_sync(0xffffffffu, pOk, i);
+                        const int l = H::leftOf(node), r = H::rightOf(l);
+                        if (!ok) {
+                            // a lent child must be back in its slot first
+                            const long long tw = clock64();
+                            if (lane == 0) {
+                                for (int k = 0; k < 2; ++k) {
+                                    const int x = k ? r : l;
+                                    unsigned long long t0 = 0;
+                                    for (unsigned it = 0; ow::lds_acq(&oc->lentState[x - firstR]) != 0; ++it)
+                                        if (!h.keep_waiting(t0, it, kSiteLockChild, x, 1)) break;
+                                }
+                            }
+                            __syncwarp();
+                            tWait += clock64() - tw;
+                            children(l, r, larger, smaller, mn);
+                        }
+                        if (c0 < mn) {
                             gen = node;
-                            oc->genL = l;
-                            oc->genR = r;
-                            oc->genLarger = larger;
-                            oc->genSmaller = smaller;
+                            if (lane == 0) {
+                                oc->genL = l;
+                                oc->genR = r;
+                                oc->genLarger = larger;
+                                oc->genSmaller = smaller;
+                            }
                             break;
                         }
-                        oc->mA[nm] = l - 1;
-                        oc->mB[nm] = r - 1;
-                        oc->mLo[nm] = node - 1;
-                        oc->mHi[nm] = larger - 1;
+                        if (lane == 0) {
+                            oc->mA[nm] = l - 1;
+                            oc->mB[nm] = r - 1;
+                            oc->mLo[nm] = node - 1;
+                            oc->mHi[nm] = larger - 1;
+                        }
                         ++nm;
                         node = smaller;
                         ++lev;
                     }
-                    oc->nm = nm;
-                    oc->gen = gen;
-                    oc->lend = (!gen && lev == R) ? node : 0;
-                    if (oc->lend) {
-                        // post the lend now: the worker's first step needs
-                        // nothing from this pass
-                        const long long tw = clock64();
-                        unsigned long long t0 = 0;
-                        for (unsigned it = 0; oc->lendReq - ow::lds_acq(&oc->lendDone) >= 4; ++it)
-                            if (!h.keep_waiting(t0, it, kSiteHandOff, -1, 0)) break;
-                        st[kStWaitRing] += clock64() - tw;
-                        ow::post_lend(oc, oc->lend, b);
-                        ++st[kStLends];
+                    if (lane == 0) {
+                        oc->nm = nm;
+                        oc->gen = gen;
+                        oc->lend = (!gen && lev == R) ? node : 0;
+                        if (oc->lend) {
+                            // post the lend now: the worker's first step needs
+                            // nothing from this pass
+                            const long long tw = clock64();
+                            unsigned long long t0 = 0;
+                            for (unsigned it = 0; oc->lendReq - ow::lds_acq(&oc->lendDone) >= 4; ++it)
+                                if (!h.keep_waiting(t0, it, kSiteHandOff, -1, 0)) break;
+                            st[kStWaitRing] += clock64() - tw;
+                            ow::post_lend(oc, oc->lend, b);
+                            ++st[kStLends];
+                        }
+                        tPass = clock64();
+                        st[kStWaitLent] += tWait;
+                        st[kStPlan] += tPass - tPlan - tWait;
+                        st[kStGeneral] += gen != 0;
                     }
-                    tPass = clock64();
-                    st[kStWaitLent] += tWait;
-                    st[kStPlan] += tPass - tPlan - tWait;
-                    st[kStGeneral] += gen != 0;
                 }
                 ow::bar_compute();
                 const int nm = oc->nm, gen = oc->gen;
@@ -467,9 +547,9 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                     K m[IPT];
                     const int q = warp / wpm;
                     const bool act = q < nm;
-                    if (act) ow::window<K, IPT>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, m);
+                    if (act) ow::window<K, IPT>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, m, scr);
                     ow::bar_compute();
-                    if (act) ow::window_store<K, IPT>(slot(oc->mLo[q]), slot(oc->mHi[q]), B, (warp - q * wpm) * S, m);
+                    if (act) ow::window_store<K, IPT>(slot(oc->mLo[q]), slot(oc->mHi[q]), B, (warp - q * wpm) * S, m, scr);
                     ow::bar_compute();
                 }
                 if (!gen) {
@@ -482,9 +562,9 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                 {
                     K m[IPT];
                     const bool act = warp < wpm;
-                    if (act) ow::window<K, IPT>(slot(oc->genL - 1), slot(oc->genR - 1), B, warp * S, m);
+                    if (act) ow::window<K, IPT>(slot(oc->genL - 1), slot(oc->genR - 1), B, warp * S, m, scr);
                     ow::bar_compute();
-                    if (act) ow::window_store<K, IPT>(slot(sT), slot(oc->genLarger - 1), B, warp * S, m);
+                    if (act) ow::window_store<K, IPT>(slot(sT), slot(oc->genLarger - 1), B, warp * S, m, scr);
                     ow::bar_compute();
                 }
                 if (ct == 0) {
@@ -509,9 +589,9 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                 } else {
                     K m[IPT];
                     const bool act = warp < wpm;
-                    if (act) ow::window<K, IPT>(C, slot(sT), B, warp * S, m);
+                    if (act) ow::window<K, IPT>(C, slot(sT), B, warp * S, m, scr);
                     ow::bar_compute();
-                    if (act) ow::window_store<K, IPT>(slot(g - 1), C, B, warp * S, m);
+                    if (act) ow::window_store<K, IPT>(slot(g - 1), C, B, warp * S, m, scr);
                 }
                 ow::bar_compute();
                 if (ct == 0) st[kStPass] += clock64() - tPass;
