@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--key", choices=["u32", "u64"], default="u32")
     p.add_argument("--dist", choices=["uniform", "sorted", "reverse", "zipf"], default="uniform")
     p.add_argument("--grid", type=int, default=0, help="blocks (0: one per SM)")
+    p.add_argument("--owner-depth", type=int, default=-1,
+                   help="owner-mode bulk delete: resident depth 2..4, 0 off, -1 automatic")
     p.add_argument("--threads", type=int, default=0, help="threads per block (0: automatic)")
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--cpu-sample-log2", type=int, default=27)
@@ -285,7 +287,8 @@ def owner_summary(st, sm_mhz):
     mhz = sm_mhz or 2070.0
     us = lambda k: round(st[k] / d / mhz, 3)
     return {"deletes": d, "lends": st["lends"], "reloads": st["reloads"], "general_steps": st["general_steps"],
-            "us_per_delete": {k: us(k) for k in ("loop", "wait_carried", "wait_lent", "wait_ring", "plan", "pass")},
+            "us_per_delete": {k: us(k) for k in ("loop", "wait_carried", "wait_lent", "wait_ring", "plan", "plan_read",
+                                                 "pass", "pass_work", "pass_sync")},
             "taker_us_per_delete": {k: us(k) for k in ("take_lock", "take_load", "take_idle")}}
 
 
@@ -320,6 +323,8 @@ def our_arm(args):
         h.set_grid(args.grid)
     if args.threads:
         h.set_block_threads(args.threads)
+    if args.owner_depth != -1:
+        h.set_owner_depth(args.owner_depth)
     h.set_timeout(args.timeout)
     info = h.info()
     torch.cuda.synchronize()

@@ -40,6 +40,7 @@ _SIGS = {
     "gh_heap_set_timeout": (_I, [_VP, ctypes.c_double]),
     "gh_heap_set_block_threads": (_I, [_VP, _I]),
     "gh_heap_set_grid": (_I, [_VP, _I]),
+    "gh_heap_set_owner_depth": (_I, [_VP, _I]),
     "gh_heap_insert": (_I, [_VP, _VP, _LL, _I, _VP]),
     "gh_heap_delete": (_I, [_VP, _VP, _LL, ctypes.POINTER(_LL), _VP]),
     "gh_heap_delete_below": (_I, [_VP, _VP, _LL, _VP, ctypes.POINTER(_LL), _VP]),
@@ -407,7 +408,11 @@ class Heap:
         _check(lib().gh_heap_restore(self._h, items.ctypes.data, c.ctypes.data), "restore")
 
     OWNER_STATS = ("deletes", "wait_carried", "wait_lent", "wait_ring", "plan", "pass", "general_steps", "loop",
-                   "take_lock", "take_load", "take_idle", "lends", "reloads")
+                   "take_lock", "take_load", "take_idle", "lends", "reloads", "plan_read", "pass_work", "pass_sync")
+
+    def set_owner_depth(self, depth):
+        """Owner-mode bulk delete depth: -1 automatic, 0 off, 2..4 resident levels."""
+        _check(lib().gh_heap_set_owner_depth(self._h, int(depth)), "set_owner_depth")
 
     def owner_stats(self):
         """Counters of the last owner-mode bulk delete (SM cycles unless a count)."""

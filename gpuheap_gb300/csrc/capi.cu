@@ -167,6 +167,7 @@ gh_status gh_heap_create(gh_heap** out, int key_kind, int variant, int partial_b
     h->d.batchNum = batch_num;
     h->d.batchSize = batch_size;
     h->d.keyBytes = kb;
+    h->d.ownerDepth = -1;
     h->d.timeoutNs = 20000000000LL;  // a starved lock wait can last a whole phase
     uint64_t bits = 0;
     if (init_limits) std::memcpy(&bits, init_limits, kb);
@@ -230,6 +231,20 @@ gh_status gh_heap_set_block_threads(gh_heap* h, int threads) {
         if (ipt != 1 && ipt != 2 && ipt != 4 && ipt != 8) return GH_ERR_INVALID;
     }
     h->blockThreads = threads;
+    return GH_OK;
+}
+
+gh_status gh_heap_set_owner_depth(gh_heap* h, int depth) {
+    if (!h) return GH_ERR_INVALID;
+    if (depth > 0) {
+        const int wpm = 2 * h->d.batchSize / (32 * gh::impl::owner_ipt(h->d.keyBytes));
+        if (!h->d.mbox || depth < 2 || depth > gh::impl::kOwnerMaxR || depth * wpm > gh::impl::kOwnerWarps ||
+            gh::impl::owner_smem(h->d.batchSize, h->d.keyBytes, depth) > 227 * 1024)
+            return GH_ERR_INVALID;
+    } else if (depth < -1) {
+        return GH_ERR_INVALID;
+    }
+    h->d.ownerDepth = depth;
     return GH_OK;
 }
 

@@ -29,6 +29,7 @@ struct Desc {
     int pb;
     int keyBytes;
     void* mbox;  // owner-mode bulk delete: mailbox + lend buffers (null: plain deleteKernel only)
+    int ownerDepth;  // owner-mode resident depth: -1 automatic, 0 off, else 2..4
 };
 
 // insertKernel: chunks of `chunk` keys, grid-strided over blocks.

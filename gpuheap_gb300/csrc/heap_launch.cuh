@@ -137,7 +137,7 @@ cudaError_t launch_insert_counted(const LaunchArgs& a, const K* keys, const unsi
 // deleteKernel alone.
 template <typename K>
 cudaError_t launch_erase(const LaunchArgs& a, K* out, const K* threshold) {
-    const int R = owner_depth(a.d->batchSize, a.d->keyBytes);
+    const int R = a.d->ownerDepth < 0 ? owner_depth(a.d->batchSize, a.d->keyBytes) : a.d->ownerDepth;
     if (!threshold && a.d->mbox && R > 0 && a.grid >= 2) {
         cudaError_t e = cudaMemsetAsync(a.d->mbox, 0, sizeof(Mailbox), a.stream);
         if (e != cudaSuccess) return e;

@@ -80,6 +80,9 @@ enum OwnerStat : int {
     kStTakeIdle,        // taker: waiting for permission or a free buffer
     kStLends,           // lends posted (count)
     kStReloads,         // lent nodes taken back (count)
+    kStPlanRead,        // compute: the plan's reads of the children (part of kStPlan)
+    kStPassWork,        // compute: warp 0's own merge windows (part of kStPass)
+    kStPassSync,        // compute: warp 0 waiting for the other windows (part of kStPass)
     kStCount = 16
 };
 
@@ -204,6 +207,17 @@ __device__ __forceinline__ void sort_regs(K (&m)[IPT]) {
 // window through `scr` (32 x 33 keys of this warp: both access patterns hit
 // 32 different banks) so that they are inside the registers too, and back;
 // IPT = 16 uses lane shuffles.  Reads shared memory only.
+template <typename K, int IPT>
+__device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (&m)[IPT], K* scr);
+
+// The 32-key window of 4-byte keys is one out-of-line function: its result
+// goes to scr, and the four places that merge share one copy of its code.
+template <typename K>
+__device__ __noinline__ void window32(const K* a, const K* b, int n, int D, K* scr) {
+    K m[32];
+    window<K, 32>(a, b, n, D, m, scr);
+}
+
 template <typename K, int IPT>
 __device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (&m)[IPT], K* scr) {
     constexpr int S = 32 * IPT;
@@ -423,7 +437,10 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
             if (H::kHasPartialBuffer && ps != 0) {
                 K m[IPT];
                 const bool act = warp < wpm;
-                if (act) ow::window<K, IPT>(C, slot(sP), B, warp * S, m, scr);
+                if (act) {
+                    if constexpr (IPT == 32) ow::window32<K>(C, slot(sP), B, warp * S, scr);
+                    else ow::window<K, IPT>(C, slot(sP), B, warp * S, m, scr);
+                }
                 ow::bar_compute();
                 if (act) ow::window_store<K, IPT>(C, slot(sP), B, warp * S, m, scr);
                 ow::bar_compute();
@@ -475,6 +492,8 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                         if (pOk) children(l, r, pLarger, pSmaller, pMin);
                     }
                     const K c0 = C[0];
+                    __syncwarp();
+                    if (lane == 0) st[kStPlanRead] += clock64() - tPlan;
                     int nm = 0, gen = 0, node = cur, lev = ow::level_of(cur);
                     while (lev < R) {
                         const int i = node - 1;
@@ -547,8 +566,17 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                     K m[IPT];
                     const int q = warp / wpm;
                     const bool act = q < nm;
-                    if (act) ow::window<K, IPT>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, m, scr);
+                    if (act) {
+                        if constexpr (IPT == 32) ow::window32<K>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, scr);
+                        else ow::window<K, IPT>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, m, scr);
+                    }
+                    const long long tw = ct == 0 ? clock64() : 0;
                     ow::bar_compute();
+                    if (ct == 0) {
+                        const long long tb = clock64();
+                        st[kStPassWork] += tw - tPass;
+                        st[kStPassSync] += tb - tw;
+                    }
                     if (act) ow::window_store<K, IPT>(slot(oc->mLo[q]), slot(oc->mHi[q]), B, (warp - q * wpm) * S, m, scr);
                     ow::bar_compute();
                 }
@@ -562,7 +590,10 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                 {
                     K m[IPT];
                     const bool act = warp < wpm;
-                    if (act) ow::window<K, IPT>(slot(oc->genL - 1), slot(oc->genR - 1), B, warp * S, m, scr);
+                    if (act) {
+                        if constexpr (IPT == 32) ow::window32<K>(slot(oc->genL - 1), slot(oc->genR - 1), B, warp * S, scr);
+                        else ow::window<K, IPT>(slot(oc->genL - 1), slot(oc->genR - 1), B, warp * S, m, scr);
+                    }
                     ow::bar_compute();
                     if (act) ow::window_store<K, IPT>(slot(sT), slot(oc->genLarger - 1), B, warp * S, m, scr);
                     ow::bar_compute();
@@ -589,7 +620,10 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                 } else {
                     K m[IPT];
                     const bool act = warp < wpm;
-                    if (act) ow::window<K, IPT>(C, slot(sT), B, warp * S, m, scr);
+                    if (act) {
+                        if constexpr (IPT == 32) ow::window32<K>(C, slot(sT), B, warp * S, scr);
+                        else ow::window<K, IPT>(C, slot(sT), B, warp * S, m, scr);
+                    }
                     ow::bar_compute();
                     if (act) ow::window_store<K, IPT>(slot(g - 1), C, B, warp * S, m, scr);
                 }
@@ -627,6 +661,7 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
             st[kStLoop] = clock64() - tLoop;
             for (int i = 0; i < 8; ++i) mb->stats[i] = st[i];
             mb->stats[kStLends] = st[kStLends];
+            for (int i = kStPlanRead; i < kStCount; ++i) mb->stats[i] = st[i];
             ow::sts_rel(&oc->stop, 1);
         }
     } else if (warp == kOwnerWarps) {

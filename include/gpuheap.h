@@ -61,6 +61,12 @@ gh_status gh_heap_set_timeout(gh_heap* h, double seconds);
 gh_status gh_heap_set_block_threads(gh_heap* h, int threads);
 /* Blocks for the bulk entry points (0 = one per SM). */
 gh_status gh_heap_set_grid(gh_heap* h, int blocks);
+/* Resident depth of the owner-mode bulk delete: -1 = automatic (the default:
+ * the deepest of 2..4 whose levels fit in one block's shared memory), 0 = off
+ * (the plain deleteKernel loop), 2..4 = levels 0..depth kept in the owner
+ * block.  It has no counterpart in the reference.  GH_ERR_INVALID when the
+ * heap has no owner mode (batch_size below 512) or the depth does not fit. */
+gh_status gh_heap_set_owner_depth(gh_heap* h, int depth);
 
 /* insertKernel (test/heap_test.cu:44-58, artifacts/synthetic/sort.cu:32-46):
  * inserts keys_dev[0, n) in insertion() calls of `chunk` keys (0 = batch_size;
