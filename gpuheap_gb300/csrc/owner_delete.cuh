@@ -120,11 +120,16 @@ inline size_t owner_smem(int batchSize, int keyBytes, int R) {
            sizeof(OwnerCtl);
 }
 // Resident depth R for a batch size and key size (0: no owner mode): the
-// deepest R <= 4 whose shared memory fits in 216 KB and whose R merges fit
-// the compute warps (one window per warp).
+// deepest R <= 2 (batch >= 2048) or 3 whose shared memory fits in 216 KB
+// and whose R merges fit the compute warps (one window per warp); depth 4
+// only when asked for (gh_heap_set_owner_depth).
 inline int owner_depth(int batchSize, int keyBytes) {
     if (batchSize < 512 || 2 * batchSize / 1024 > 8) return 0;
-    for (int R = kOwnerMaxR; R >= 2; --R) {
+    // measured on GB300 (2^26 u32 keys): at batch 2048 depth 2 takes 4.5 us
+    // per delete against 5.4 at depth 3 (the merges of a deeper pass cost
+    // more than the lent nodes it saves waiting for); at 1024, 3 beats 4
+    const int top = batchSize >= 2048 ? 2 : 3;
+    for (int R = top; R >= 2; --R) {
         const int windows = R * (2 * batchSize / (32 * owner_ipt(keyBytes)));
         if (owner_smem(batchSize, keyBytes, R) <= 216 * 1024 && windows <= kOwnerWarps && windows >= R) return R;
     }
@@ -140,11 +145,14 @@ namespace ow {
 __device__ __forceinline__ void bar_compute() {
     asm volatile("bar.sync 1, %0;" ::"r"(kOwnerWarps * 32) : "memory");
 }
-__device__ __forceinline__ int lds_acq(const int* p) {
+// Polls read shared words relaxed and fence once they see what they wait
+// for (fence_acq): an acquire on every poll would fence on every poll.
+__device__ __forceinline__ int lds(const int* p) {
     int v;
-    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(detail::smem_u32(p)) : "memory");
+    asm volatile("ld.relaxed.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(detail::smem_u32(p)) : "memory");
     return v;
 }
+__device__ __forceinline__ void fence_acq() { asm volatile("fence.acq_rel.cta;" ::: "memory"); }
 __device__ __forceinline__ void sts_rel(int* p, int v) {
     asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(detail::smem_u32(p)), "r"(v) : "memory");
 }
@@ -207,17 +215,6 @@ __device__ __forceinline__ void sort_regs(K (&m)[IPT]) {
 // window through `scr` (32 x 33 keys of this warp: both access patterns hit
 // 32 different banks) so that they are inside the registers too, and back;
 // IPT = 16 uses lane shuffles.  Reads shared memory only.
-template <typename K, int IPT>
-__device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (&m)[IPT], K* scr);
-
-// The 32-key window of 4-byte keys is one out-of-line function: its result
-// goes to scr, and the four places that merge share one copy of its code.
-template <typename K>
-__device__ __noinline__ void window32(const K* a, const K* b, int n, int D, K* scr) {
-    K m[32];
-    window<K, 32>(a, b, n, D, m, scr);
-}
-
 template <typename K, int IPT>
 __device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (&m)[IPT], K* scr) {
     constexpr int S = 32 * IPT;
@@ -420,10 +417,11 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                     const long long tw = clock64();
                     unsigned long long t0 = 0;
                     for (unsigned it = 0;; ++it) {
-                        if (ow::lds_acq(&oc->cReady[b]) == d + 1) break;
-                        if (ow::lds_acq(&oc->cEnd) == d) { stop = 1; break; }
+                        if (ow::lds(&oc->cReady[b]) == d + 1) break;
+                        if (ow::lds(&oc->cEnd) == d) { stop = 1; break; }
                         if (!h.keep_waiting(t0, it, kSiteLockLast, -1, d)) { stop = 1; break; }
                     }
+                    ow::fence_acq();
                     st[kStWaitCarried] += clock64() - tw;
                 }
                 // the next delete's last node may be taken during this one
@@ -437,10 +435,7 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
             if (H::kHasPartialBuffer && ps != 0) {
                 K m[IPT];
                 const bool act = warp < wpm;
-                if (act) {
-                    if constexpr (IPT == 32) ow::window32<K>(C, slot(sP), B, warp * S, scr);
-                    else ow::window<K, IPT>(C, slot(sP), B, warp * S, m, scr);
-                }
+                if (act) ow::window<K, IPT>(C, slot(sP), B, warp * S, m, scr);
                 ow::bar_compute();
                 if (act) ow::window_store<K, IPT>(C, slot(sP), B, warp * S, m, scr);
                 ow::bar_compute();
@@ -488,8 +483,11 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                     if (lane < firstR - 1) {
                         const int v = lane + 1, l = H::leftOf(v), r = H::rightOf(l);
                         pOk = ow::level_of(l) < R ||
-                              (ow::lds_acq(&oc->lentState[l - firstR]) == 0 && ow::lds_acq(&oc->lentState[r - firstR]) == 0);
-                        if (pOk) children(l, r, pLarger, pSmaller, pMin);
+                              (ow::lds(&oc->lentState[l - firstR]) == 0 && ow::lds(&oc->lentState[r - firstR]) == 0);
+                        if (pOk) {
+                            if (ow::level_of(l) == R) ow::fence_acq();  // after the reloads' completion
+                            children(l, r, pLarger, pSmaller, pMin);
+                        }
                     }
                     const K c0 = C[0];
                     __syncwarp();
@@ -509,9 +507,10 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                                 for (int k = 0; k < 2; ++k) {
                                     const int x = k ? r : l;
                                     unsigned long long t0 = 0;
-                                    for (unsigned it = 0; ow::lds_acq(&oc->lentState[x - firstR]) != 0; ++it)
+                                    for (unsigned it = 0; ow::lds(&oc->lentState[x - firstR]) != 0; ++it)
                                         if (!h.keep_waiting(t0, it, kSiteLockChild, x, 1)) break;
                                 }
+                                ow::fence_acq();
                             }
                             __syncwarp();
                             tWait += clock64() - tw;
@@ -546,7 +545,7 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                             // nothing from this pass
                             const long long tw = clock64();
                             unsigned long long t0 = 0;
-                            for (unsigned it = 0; oc->lendReq - ow::lds_acq(&oc->lendDone) >= 4; ++it)
+                            for (unsigned it = 0; oc->lendReq - ow::lds(&oc->lendDone) >= 4; ++it)
                                 if (!h.keep_waiting(t0, it, kSiteHandOff, -1, 0)) break;
                             st[kStWaitRing] += clock64() - tw;
                             ow::post_lend(oc, oc->lend, b);
@@ -566,10 +565,7 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                     K m[IPT];
                     const int q = warp / wpm;
                     const bool act = q < nm;
-                    if (act) {
-                        if constexpr (IPT == 32) ow::window32<K>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, scr);
-                        else ow::window<K, IPT>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, m, scr);
-                    }
+                    if (act) ow::window<K, IPT>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, m, scr);
                     const long long tw = ct == 0 ? clock64() : 0;
                     ow::bar_compute();
                     if (ct == 0) {
@@ -590,10 +586,7 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                 {
                     K m[IPT];
                     const bool act = warp < wpm;
-                    if (act) {
-                        if constexpr (IPT == 32) ow::window32<K>(slot(oc->genL - 1), slot(oc->genR - 1), B, warp * S, scr);
-                        else ow::window<K, IPT>(slot(oc->genL - 1), slot(oc->genR - 1), B, warp * S, m, scr);
-                    }
+                    if (act) ow::window<K, IPT>(slot(oc->genL - 1), slot(oc->genR - 1), B, warp * S, m, scr);
                     ow::bar_compute();
                     if (act) ow::window_store<K, IPT>(slot(sT), slot(oc->genLarger - 1), B, warp * S, m, scr);
                     ow::bar_compute();
@@ -620,10 +613,7 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                 } else {
                     K m[IPT];
                     const bool act = warp < wpm;
-                    if (act) {
-                        if constexpr (IPT == 32) ow::window32<K>(C, slot(sT), B, warp * S, scr);
-                        else ow::window<K, IPT>(C, slot(sT), B, warp * S, m, scr);
-                    }
+                    if (act) ow::window<K, IPT>(C, slot(sT), B, warp * S, m, scr);
                     ow::bar_compute();
                     if (act) ow::window_store<K, IPT>(slot(g - 1), C, B, warp * S, m, scr);
                 }
@@ -637,7 +627,7 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                     if (ct == 0) {
                         const long long tw = clock64();
                         unsigned long long t0 = 0;
-                        for (unsigned it = 0; oc->lendReq - ow::lds_acq(&oc->lendDone) >= 4; ++it)
+                        for (unsigned it = 0; oc->lendReq - ow::lds(&oc->lendDone) >= 4; ++it)
                             if (!h.keep_waiting(t0, it, kSiteHandOff, -1, 0)) break;
                         st[kStWaitRing] += clock64() - tw;
                         ow::post_lend(oc, cur, b);
@@ -675,11 +665,12 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                 const long long ti = clock64();
                 unsigned long long t0 = 0;
                 for (unsigned it = 0;; ++it) {
-                    if (ow::lds_acq(&oc->stop)) break;
-                    if (ow::lds_acq(&oc->takeAllowed) > t && ow::lds_acq(&oc->cFree[b]) >= (t >> 1)) { go = 1; break; }
+                    if (ow::lds(&oc->stop)) break;
+                    if (ow::lds(&oc->takeAllowed) > t && ow::lds(&oc->cFree[b]) >= (t >> 1)) { go = 1; break; }
                     if (!h.keep_waiting(t0, it, kSiteLockLast, -1, t)) break;
                     __nanosleep(32);
                 }
+                ow::fence_acq();
                 tkIdle += clock64() - ti;
                 if (go && bc < (2 << R)) {  // the last node would be resident: the owner is done
                     ow::sts_rel(&oc->cEnd, t);
@@ -742,11 +733,15 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
             if (lane == 0) {
                 unsigned long long t0 = 0;
                 for (unsigned it = 0;; ++it) {
-                    if (ow::lds_acq(&oc->lendReq) > q) { go = 1; break; }
-                    if (ow::lds_acq(&oc->stop) && ow::lds_acq(&oc->lendReq) <= q) break;
+                    if (ow::lds(&oc->lendReq) > q) { go = 1; break; }
+                    if (ow::lds(&oc->stop)) {
+                        ow::fence_acq();
+                        if (ow::lds(&oc->lendReq) <= q) break;
+                    }
                     if (!h.keep_waiting(t0, it, kSiteHandOff, -1, q)) break;
                     __nanosleep(32);
                 }
+                ow::fence_acq();
                 if (go) {
                     // the entry's previous lend must have been read by its worker
                     const int e = q % kMboxEntries;
@@ -790,10 +785,11 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
         for (;;) {
             // `stop` first: the compute warps mark their last lend before they
             // set it, so a scan that follows a seen `stop` finds every lend
-            const int stop = __shfl_sync(0xffffffffu, lane == 0 ? ow::lds_acq(&oc->stop) : 0, 0);
+            const int stop = __shfl_sync(0xffffffffu, lane == 0 ? ow::lds(&oc->stop) : 0, 0);
+            ow::fence_acq();
             int st = 0;
             if (lane < nR) {
-                st = ow::lds_acq(&oc->lentState[lane]);
+                st = ow::lds(&oc->lentState[lane]);
                 if (st == 1) {
                     const int x = firstR + lane;
                     if (detail::ld_relaxed(h.status + x) == 0 && detail::cas_acquire(h.status + x, 0, L) == 0) {
