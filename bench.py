@@ -287,7 +287,6 @@ def owner_summary(st, sm_mhz):
     mhz = sm_mhz or 2070.0
     us = lambda k: round(st[k] / d / mhz, 3)
     return {"deletes": d, "lends": st["lends"], "reloads": st["reloads"], "general_steps": st["general_steps"],
-            "planned_ahead": st.get("planned_ahead", 0),
             "us_per_delete": {k: us(k) for k in ("loop", "wait_carried", "wait_lent", "wait_ring", "plan", "plan_read",
                                                  "pass", "pass_work", "pass_sync")},
             "taker_us_per_delete": {k: us(k) for k in ("take_lock", "take_load", "take_idle")}}

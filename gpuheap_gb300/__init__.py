@@ -408,8 +408,7 @@ class Heap:
         _check(lib().gh_heap_restore(self._h, items.ctypes.data, c.ctypes.data), "restore")
 
     OWNER_STATS = ("deletes", "wait_carried", "wait_lent", "wait_ring", "plan", "pass", "general_steps", "loop",
-                   "take_lock", "take_load", "take_idle", "lends", "reloads", "plan_read", "pass_work", "pass_sync",
-                   "planned_ahead")
+                   "take_lock", "take_load", "take_idle", "lends", "reloads", "plan_read", "pass_work", "pass_sync")
 
     def set_owner_depth(self, depth):
         """Owner-mode bulk delete depth: -1 automatic, 0 off, 2..4 resident levels."""

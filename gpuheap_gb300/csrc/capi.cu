@@ -238,7 +238,7 @@ gh_status gh_heap_set_owner_depth(gh_heap* h, int depth) {
     if (!h) return GH_ERR_INVALID;
     if (depth > 0) {
         const int wpm = 2 * h->d.batchSize / (32 * gh::impl::owner_ipt(h->d.keyBytes));
-        if (!h->d.mbox || depth < 2 || depth > gh::impl::kOwnerMaxR || depth * wpm > gh::impl::kOwnerWarps - 1 ||
+        if (!h->d.mbox || depth < 2 || depth > gh::impl::kOwnerMaxR || depth * wpm > gh::impl::kOwnerWarps ||
             gh::impl::owner_smem(h->d.batchSize, h->d.keyBytes, depth) > 227 * 1024)
             return GH_ERR_INVALID;
     } else if (depth < -1) {

@@ -62,7 +62,7 @@ struct alignas(128) Mailbox {
     int seq[kMboxEntries];   // entry e holds lend q once seq[e] == q + 1
     int cons[kMboxEntries];  // uses of entry e that a worker has read
     int node[kMboxEntries];  // the level-R node lent with it
-    unsigned long long stats[24];  // counters of the launch, indexed by OwnerStat
+    unsigned long long stats[16];  // counters of the launch, indexed by OwnerStat
 };
 
 // Indices of Mailbox::stats (SM cycles unless a count).
@@ -83,13 +83,12 @@ enum OwnerStat : int {
     kStPlanRead,        // compute: the plan's reads of the children (part of kStPlan)
     kStPassWork,        // compute: warp 0's own merge windows (part of kStPass)
     kStPassSync,        // compute: warp 0 waiting for the other windows (part of kStPass)
-    kStPlanAhead,       // deletes whose plan was made during the previous delete's pass (count)
-    kStCount = 24
+    kStCount = 16
 };
 
 // Shared-memory control words of the owner block (after its node slots).
 struct alignas(16) OwnerCtl {
-    unsigned long long st[24];                  // counters (OwnerStat), compute thread 0
+    unsigned long long st[16];                  // counters (OwnerStat), compute thread 0
     unsigned long long cbar[2];                 // bulk loads of the two carried-batch buffers
     unsigned long long rbar[1 << kOwnerMaxR];   // bulk reloads of lent level-R nodes
     unsigned long long sbar;                    // set-up loads
@@ -109,12 +108,7 @@ struct alignas(16) OwnerCtl {
     int plStop, nm, gen, genL, genR, genLarger, genSmaller, lend;
     int mA[kOwnerMaxR], mB[kOwnerMaxR], mLo[kOwnerMaxR], mHi[kOwnerMaxR];
     int caseSel;
-    // plan of the next delete, made during this delete's pass (nxValid = 1)
-    int nxValid, nxLend;
-    int nxA[kOwnerMaxR], nxB[kOwnerMaxR], nxLo[kOwnerMaxR], nxHi[kOwnerMaxR];
 };
-
-constexpr int kPlanWarp = kOwnerWarps - 1;  // the compute warp that plans ahead (never a merge window)
 
 // Transpose scratch of one merge window (32 x 33 keys, one pad column).
 inline size_t owner_scratch(int keyBytes) { return owner_ipt(keyBytes) == 32 ? 32 * 33 * keyBytes : 0; }
@@ -137,7 +131,7 @@ inline int owner_depth(int batchSize, int keyBytes) {
     const int top = batchSize >= 2048 ? 2 : 3;
     for (int R = top; R >= 2; --R) {
         const int windows = R * (2 * batchSize / (32 * owner_ipt(keyBytes)));
-        if (owner_smem(batchSize, keyBytes, R) <= 216 * 1024 && windows <= kOwnerWarps - 1 && windows >= R) return R;
+        if (owner_smem(batchSize, keyBytes, R) <= 216 * 1024 && windows <= kOwnerWarps && windows >= R) return R;
     }
     return 0;
 }
@@ -283,91 +277,6 @@ __device__ __forceinline__ void post_lend(OwnerCtl* oc, int node, int buf) {
 
 }  // namespace ow
 
-// ---------------------------------------------------------------- plan ahead
-// Plans the next delete's path while this delete's pass runs (the whole
-// planner warp, warp-uniform; lane 0 writes oc->nx*).  The pass writes only
-// the nodes on this delete's path v_0..v_{R-1} (lo of their children) and
-// the larger child of each (hi); their next first and last keys come from
-// one merge-path split at diagonal B per level, read before the pass writes.
-// Every other resident node keeps its keys.  Gives up (false) when the
-// next path needs the node this delete lends out, a lent node, or the
-// general sift step; the next delete then plans after this pass as usual.
-template <typename H, typename K>
-__device__ __noinline__ bool plan_ahead(const H& h, OwnerCtl* oc, const K* slots, int R, K c0) {
-    const int B = h.batchSize;
-    const int lane = threadIdx.x & 31;
-    const int firstR = 1 << R;
-    auto slot = [&](int s) -> const K* { return slots + static_cast<size_t>(s) * B; };
-    K loF[kOwnerMaxR], loL[kOwnerMaxR], hiF[kOwnerMaxR], hiL[kOwnerMaxR];
-    int vpath[kOwnerMaxR + 1], lg[kOwnerMaxR];
-    for (int j = 0; j < R; ++j) {
-        const K* X = slot(oc->mA[j]);
-        const K* Y = slot(oc->mB[j]);
-        const int i = ow::warp_split(X, Y, B, B);  // X's keys among the B smallest
-        const int jy = B - i;
-        const K x0 = X[0], y0 = Y[0], xl = X[B - 1], yl = Y[B - 1];
-        loF[j] = x0 < y0 ? x0 : y0;
-        if (i == 0) loL[j] = Y[B - 1];
-        else if (jy == 0) loL[j] = xl;
-        else { const K u = X[i - 1], v = Y[jy - 1]; loL[j] = u < v ? v : u; }
-        if (i == B) hiF[j] = y0;
-        else if (jy == B) hiF[j] = x0;
-        else { const K u = X[i], v = Y[jy]; hiF[j] = u < v ? u : v; }
-        hiL[j] = xl < yl ? yl : xl;
-        vpath[j] = oc->mLo[j] + 1;
-        lg[j] = oc->mHi[j] + 1;
-    }
-    vpath[R] = oc->lend;
-    int nA[kOwnerMaxR], nB[kOwnerMaxR], nLo[kOwnerMaxR], nHi[kOwnerMaxR];
-    int node = 1;
-    bool onPath = true;
-    for (int lev = 0; lev < R; ++lev) {
-        const int l = H::leftOf(node), r = H::rightOf(l);
-        K f[2], la[2];
-        for (int k = 0; k < 2; ++k) {
-            const int c = k ? r : l;
-            if (onPath) {
-                // node is this delete's v_lev: its children are v_{lev+1} and the larger one
-                if (c == vpath[lev + 1]) {
-                    if (lev + 1 == R) return false;  // lent by this delete
-                    f[k] = loF[lev + 1];
-                    la[k] = loL[lev + 1];
-                } else {
-                    f[k] = hiF[lev];
-                    la[k] = hiL[lev];
-                }
-            } else {
-                if (ow::level_of(c) == R) {
-                    if (ow::lds(&oc->lentState[c - firstR]) != 0) return false;
-                    ow::fence_acq();
-                }
-                f[k] = slot(c - 1)[0];
-                la[k] = slot(c - 1)[B - 1];
-            }
-        }
-        const int larger = (la[0] < la[1] || (la[0] == la[1] && !(la[0] < h.init_limits) && f[0] < f[1])) ? r : l;
-        const int smaller = larger == r ? l : r;
-        if (c0 < (la[0] < la[1] ? la[0] : la[1])) return false;  // the general step: plan it after the pass
-        nA[lev] = l - 1;
-        nB[lev] = r - 1;
-        nLo[lev] = node - 1;
-        nHi[lev] = larger - 1;
-        onPath = onPath && smaller == vpath[lev + 1];
-        node = smaller;
-    }
-    if (lane == 0) {
-        for (int j = 0; j < R; ++j) {
-            oc->nxA[j] = nA[j];
-            oc->nxB[j] = nB[j];
-            oc->nxLo[j] = nLo[j];
-            oc->nxHi[j] = nHi[j];
-        }
-        oc->nxLend = node;
-    }
-    __syncwarp();
-    return true;
-}
-
 // ---------------------------------------------------------------- workers
 // Blocks 1.. of the launch: take lends in order, load the carried batch and
 // run deleteUpdate's sift from the lent node (heap/tditdd/heap.cuh:418-532,
@@ -437,7 +346,6 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
         oc->cEnd = -1;
         oc->lendReq = oc->lendDone = 0;
         oc->stop = 0;
-        oc->nxValid = 0;
         oc->plStop = 0;
         for (int i = 0; i < (1 << kOwnerMaxR); ++i) oc->lentState[i] = 0;
         const int bc = detail::ld_relaxed(&h.state->batchCount);
@@ -551,32 +459,7 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
             int lendNode = 0;
             for (;;) {
                 long long tPass = 0;
-                const int adopt = cur == 1 && oc->nxValid;  // read by every thread before any write below
-                if (warp == 0 && adopt) {
-                    // the plan made ahead during the previous delete's pass
-                    const long long tPlan = clock64();
-                    if (lane == 0) {
-                        for (int j = 0; j < R; ++j) {
-                            oc->mA[j] = oc->nxA[j];
-                            oc->mB[j] = oc->nxB[j];
-                            oc->mLo[j] = oc->nxLo[j];
-                            oc->mHi[j] = oc->nxHi[j];
-                        }
-                        oc->nm = R;
-                        oc->gen = 0;
-                        oc->lend = oc->nxLend;
-                        const long long tw = clock64();
-                        unsigned long long t0 = 0;
-                        for (unsigned it = 0; oc->lendReq - ow::lds(&oc->lendDone) >= 4; ++it)
-                            if (!h.keep_waiting(t0, it, kSiteHandOff, -1, 0)) break;
-                        st[kStWaitRing] += clock64() - tw;
-                        ow::post_lend(oc, oc->lend, b);
-                        ++st[kStLends];
-                        ++st[kStPlanAhead];
-                        tPass = clock64();
-                        st[kStPlan] += tPass - tPlan;
-                    }
-                } else if (warp == 0) {
+                if (warp == 0) {
                     const long long tPlan = clock64();
                     long long tWait = 0;
                     // plan: follow the smaller child while the carried batch
@@ -683,17 +566,6 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                     const int q = warp / wpm;
                     const bool act = q < nm;
                     if (act) ow::window<K, IPT>(slot(oc->mA[q]), slot(oc->mB[q]), B, (warp - q * wpm) * S, m, scr);
-                    if (warp == kPlanWarp) {
-                        // meanwhile, plan the next delete from what this pass
-                        // will write (reads done before the barrier below)
-                        int ok = cur == 1 && !gen && oc->lend && ps == 0 && dc + 2 * B <= lim;
-                        if (ok) ok = ow::lds(&oc->cReady[b ^ 1]) == d + 2;
-                        if (ok) {
-                            ow::fence_acq();
-                            ok = plan_ahead(h, oc, slots, R, slot(sC + (b ^ 1))[0]);
-                        }
-                        if (lane == 0) oc->nxValid = ok;
-                    }
                     const long long tw = ct == 0 ? clock64() : 0;
                     ow::bar_compute();
                     if (ct == 0) {
@@ -779,7 +651,6 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
             st[kStLoop] = clock64() - tLoop;
             for (int i = 0; i < 8; ++i) mb->stats[i] = st[i];
             mb->stats[kStLends] = st[kStLends];
-            mb->stats[kStPlanAhead] = st[kStPlanAhead];
             for (int i = kStPlanRead; i < kStCount; ++i) mb->stats[i] = st[i];
             ow::sts_rel(&oc->stop, 1);
         }

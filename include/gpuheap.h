@@ -382,9 +382,7 @@ long long gh_launch_count(void);
  * come back, [3] waiting for room to lend, [4] planning paths, [5] merging;
  * [6] general sift steps; [7] cycles of the whole loop; the last-node taker's
  * cycles [8] in lock waits, [9] in bulk loads, [10] idle; [11] lends;
- * [12] lent nodes taken back; [13] cycles of the plans' reads, of the
- * passes [14] merging and [15] waiting for the slowest window (one warp's
- * view); [16] deletes whose plan was made during the previous pass.  Synchronizes the device.  All zero when the
+ * [12] lent nodes taken back.  Synchronizes the device.  All zero when the
  * heap has no owner mode (batch_size below 512) or none has run. */
 gh_status gh_heap_owner_stats(gh_heap* h, unsigned long long* out, int n);
 
