@@ -13,7 +13,6 @@
 #include <climits>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "gpuheap.h"
 #include "heap_launch.cuh"
@@ -25,28 +24,20 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = size_t{16} << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_ptr[kMaxDevices] = {};
-
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-// Device address of the array on the current device, looked up once per
-// device (the host-side symbol is only a stand-in and must never reach a kernel).
+// Device address of the array on the current device (the host-side symbol
+// is only a stand-in and must never reach a kernel).  Looked up on every
+// call, with the device current: a cached address would dangle after a
+// device reset reloads the module, and the lookup costs little next to a sort.
 gh_status scratch_for_current_device(void** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GH_ERR_CUDA;
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            std::fprintf(stderr, "gpuheap: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
-            return GH_ERR_CUDA;
-        }
-        g_scratch_ptr[dev] = p;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        std::fprintf(stderr, "gpuheap: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+        return GH_ERR_CUDA;
     }
-    *out = g_scratch_ptr[dev];
+    *out = p;
     return GH_OK;
 }
 
@@ -81,6 +72,13 @@ extern "C" gh_status gh_sort_noalloc(int key_kind, int variant, int partial_buff
     if (variant != GH_TOPDOWN && variant != GH_BOTTOMUP) return GH_ERR_INVALID;
     if (batch_size < 16 || batch_size > 4096 || (batch_size & (batch_size - 1))) return GH_ERR_INVALID;
     if (n < 0 || (n > 0 && (!in_dev || !out_dev))) return GH_ERR_INVALID;
+    // without the partial buffer a short last batch is padded to a full node
+    // and its keys come out only with that padding, past out_dev's n keys
+    if (!partial_buffer && n % batch_size != 0) {
+        std::fprintf(stderr, "gpuheap: gh_sort_noalloc: without the partial buffer n (%lld) must be a multiple of "
+                             "batch_size (%d)\n", n, batch_size);
+        return GH_ERR_INVALID;
+    }
     if (n == 0) return GH_OK;
     const int kb = key_kind == GH_KEY_U64 ? 8 : 4;
     const long long nodes = (n + batch_size - 1) / batch_size;  // full nodes a sort of n keys can hold

@@ -195,9 +195,12 @@ size_t gh_heap_smem_bytes(int key_kind, int batch_size);
  * until the process exits); only in_dev and out_dev come from the caller.
  * Limit: the heap needs ((ceil(n / batch_size) + 1) * batch_size * key bytes,
  * rounded up to 256) + (4 * (ceil(n / batch_size) + 2), rounded up to 256) +
- * 256 bytes <= 16 MiB, e.g. about 4.1 M u32 keys at batch_size 1024; larger
- * n returns GH_ERR_CAPACITY and prints the sizes.  The first call on each
- * device looks up the array's device address (cudaGetSymbolAddress); make
+ * 384 bytes (the counters) <= 16 MiB, e.g. about 4.1 M u32 keys at
+ * batch_size 1024; larger n returns GH_ERR_CAPACITY and prints the sizes.
+ * Without the partial buffer, n must be a multiple of batch_size
+ * (GH_ERR_INVALID otherwise: a padded last batch would not fit out_dev).
+ * Every call looks up the array's device address on the current device
+ * (cudaGetSymbolAddress); the first call on a device also loads it, so make
  * that first call before any stream capture.  Every call reuses the same
  * array (cleared at the start of each call), so calls whose work overlaps
  * on the GPU -- other streams, other host threads -- race: serialize them.

@@ -52,9 +52,19 @@ void* create_t(int batchNum, int batchSize, K init) {
     return b;
 }
 
+// Every call starts from the same shared-memory stand-in and spin counter.
+// Both are process-wide and would otherwise carry one call's leftovers into
+// the next, so that a fixed operation sequence could end differently
+// depending on what ran before it in the same process.
+inline void fresh_call() {
+    std::memset(REF_NS::s, 0, sizeof(REF_NS::s));
+    g_shim_fail_streak = 0;
+}
+
 template <typename K>
 int insert_t(void* hb, const K* items, int size) {
     auto* b = static_cast<Box<K>*>(hb);
+    fresh_call();
     try {
         b->h->insertion(const_cast<K*>(items), size, 0);
     } catch (const ShimSpinError&) {
@@ -67,6 +77,7 @@ template <typename K>
 int delete_t(void* hb, K* out, int* size) {
     auto* b = static_cast<Box<K>*>(hb);
     int sz = 0;
+    fresh_call();
     try {
         if (b->h->deleteRoot(out, sz)) b->h->deleteUpdate(0);
     } catch (const ShimSpinError&) {

@@ -14,7 +14,7 @@ scenario) and `large` (bgpq_ref_cases_large.npz, batch 256-2048, the batch
 sizes of the heap-sort configurations).
 
 Usage (needs the reference tree; not run by the tests):
-    make -C oracle ref && python tests/golden/make_golden.py [small] [large]
+    make -C oracle ref REF=<reference tree> && python tests/golden/make_golden.py [small] [large]
 """
 import ctypes
 import json
