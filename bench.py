@@ -53,10 +53,10 @@ def parse():
                    help="owner-mode bulk delete: resident depth 2..4, 0 off, -1 automatic")
     p.add_argument("--threads", type=int, default=0, help="threads per block (0: automatic)")
     p.add_argument("--seed", type=int, default=2026)
-    p.add_argument("--cpu-sample-log2", type=int, default=27)
+    p.add_argument("--cpu-sample-log2", type=int, default=28)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--timeout", type=float, default=20.0,
+    p.add_argument("--timeout", type=float, default=2.0,
                    help="device wait limit in seconds (raise it under a profiler)")
     p.add_argument("--workload", choices=["heapsort", "sssp", "batched", "served", "fifo"], default="heapsort",
                    help="heapsort: the plain heap-sort line (default); sssp: SSSP with the queue; "

@@ -168,7 +168,7 @@ gh_status gh_heap_create(gh_heap** out, int key_kind, int variant, int partial_b
     h->d.batchSize = batch_size;
     h->d.keyBytes = kb;
     h->d.ownerDepth = -1;
-    h->d.timeoutNs = 20000000000LL;  // a starved lock wait can last a whole phase
+    h->d.timeoutNs = 2000000000LL;  // 2 s: bulk deletes queue for node 0 in order, bulk inserts reserve targets
     uint64_t bits = 0;
     if (init_limits) std::memcpy(&bits, init_limits, kb);
     else if (key_kind == GH_KEY_U32) bits = 0xffffffffull;

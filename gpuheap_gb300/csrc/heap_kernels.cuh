@@ -105,10 +105,15 @@ __device__ __forceinline__ int delete_one(const H& h, K* out) {
 
 // deleteKernel: every block deletes until the heap is empty, or (check)
 // its smallest key is not below `threshold` (deleteRoot's app_t_val), or
-// the output limit / an error stops it.
+// the output limit / an error stops it.  The blocks queue for node 0 by
+// ticket (deleteRoot's `fair`), so none starves.
 template <typename H, typename K>
 __global__ void __launch_bounds__(1024) k_delete(H h, K* out, K threshold, int check) {
-    while (delete_one(h, out, threshold, check != 0) != 0) {}
+    for (;;) {
+        int size = 0;
+        h.deleteMinImpl(out, size, threshold, check != 0, 0, true);
+        if (size == 0) break;
+    }
 }
 
 // concurrentKernel (test/heap_test.cu:13-38): the first half of the grid
@@ -168,6 +173,8 @@ static __global__ void k_init_state(HeapState* st, int deleteCount) {
         st->resvBase = 0;
         st->resvCount = 0;
         st->resvTurn = 0;
+        st->delTicket = 0;
+        st->delServing = 0;
         st->err = 0;
         st->errOp = 0;
         st->errNode = 0;
@@ -182,6 +189,8 @@ static __global__ void k_set_output(HeapState* st, int deleteCount, int outLimit
     if (threadIdx.x == 0) {
         if (deleteCount >= 0) st->deleteCount = deleteCount;
         st->outLimit = outLimit;
+        st->delTicket = 0;
+        st->delServing = 0;
     }
 }
 

@@ -49,11 +49,12 @@ gh_status gh_heap_destroy(gh_heap* h);
 /* reset(): heap/tditdd/heap.cuh:69-91 (also clears a recorded device error). */
 gh_status gh_heap_reset(gh_heap* h, void* stream);
 
-/* Time limit of every device-side wait, in (0, 60] seconds (default 20 s).
- * The node locks are not fair: under contention one block's wait can last
- * as long as a whole phase of the others' work (a 2^28-key heap-sort at
- * batch 512 spends 2.3 s in its deletes), so the limit is well above that;
- * it exists to turn a hang into GH_ERR_TIMEOUT. */
+/* Time limit of every device-side wait, in (0, 60] seconds (default 2 s).
+ * It turns a hang into GH_ERR_TIMEOUT.  The bulk drivers keep every wait
+ * short: a bulk insert reserves its targets (no race for node 0), the blocks
+ * of a bulk delete queue for node 0 by ticket, and an owner-mode delete's
+ * waits last a few deletes.  Single operations and application kernels that
+ * race many blocks on one heap's node 0 may need a longer limit. */
 gh_status gh_heap_set_timeout(gh_heap* h, double seconds);
 /* Threads per block for the bulk entry points (0 = automatic: 16-byte merge
  * runs per thread); a power of two in [32, 1024] with 2*batch_size/threads

@@ -83,7 +83,9 @@ struct alignas(128) HeapState {
     int resvBase;           // bulk insert: targets resvBase+1 .. resvBase+resvCount are reserved
     int resvCount;          // 0: no reservation (the bulk insert takes node 0 per batch)
     int resvTurn;           // top-down reserved inserts take the root in target order: the next target
-    int pad2[11];
+    int delTicket;          // bulk deletes: next ticket for node 0 (atomicAdd)
+    int delServing;         // bulk deletes: the ticket whose holder may lock node 0 now
+    int pad2[9];
     unsigned long long appStats[8];  // applications: counters (e.g. pops, expansions, relaxations)
 };
 
@@ -890,6 +892,19 @@ struct Heap {
         if (tid == 0) unlock(1, BU::AVAIL);  // (:685-688)
     }
 
+    // Thread 0 of a bulk-delete block: draws a ticket and waits (bounded)
+    // until it is served, so that the blocks of a bulk delete take node 0 in
+    // the order they asked for it.  Unlike racing on node 0's lock word, no
+    // block can lose to the others for a whole phase.  Returns the ticket
+    // (passed on with delServing once node 0 is held), or -2 on a failed wait.
+    __device__ __forceinline__ int takeTurn() const {
+        const int t = atomicAdd(&state->delTicket, 1);
+        unsigned long long t0 = 0;
+        for (unsigned it = 0; detail::ld_acquire(&state->delServing) != t; ++it)
+            if (!keep_waiting(t0, it, kSiteLockPartial, 0, t)) return -2;
+        return t;
+    }
+
     // Thread 0: waits (bounded) until the reserved-insert turn reaches `target`.
     __device__ __forceinline__ bool waitTurn(int target) const {
         unsigned long long t0 = 0;
@@ -920,7 +935,10 @@ struct Heap {
 
     // `check` false: no threshold at all (heap/tditdd/heap.cuh:267), so a heap
     // without the partial buffer also gives up its padding batches.
-    __device__ __forceinline__ bool deleteRootImpl(K* items, int& size, K threshold, bool check) const {
+    // `fair`: the caller is one of many blocks of a bulk delete; it queues for
+    // node 0 by ticket (takeTurn) instead of racing on the lock word.
+    __device__ __forceinline__ bool deleteRootImpl(K* items, int& size, K threshold, bool check,
+                                                   bool fair = false) const {
         __shared__ OpCtl dr;
         OpCtl* c = &dr;
         size = 0;
@@ -929,7 +947,9 @@ struct Heap {
         __syncthreads();
         if (tid == 0) {
             c->w[0] = 0;  // 0: nothing, 1: partial buffer only, 2: root
-            const bool ok = detail::ld_relaxed(&state->err) == 0 && lock(0, 0, L, kSiteLockPartial);
+            const int turn = fair ? takeTurn() : -1;
+            const bool ok = turn != -2 && detail::ld_relaxed(&state->err) == 0 && lock(0, 0, L, kSiteLockPartial);
+            if (turn >= 0) detail::st_release(&state->delServing, turn + 1);
             c->abort = !ok;
             if (ok) {
                 const int bc = detail::ld_relaxed(&state->batchCount);
@@ -1034,16 +1054,17 @@ struct Heap {
     __device__ __forceinline__ void deleteMin(K* items, int& size, int smemOffset) const {
         deleteMinImpl(items, size, init_limits, false, smemOffset);
     }
-    __device__ __forceinline__ void deleteMinImpl(K* items, int& size, K threshold, bool check, int smemOffset) const {
+    __device__ __forceinline__ void deleteMinImpl(K* items, int& size, K threshold, bool check, int smemOffset,
+                                                  bool fair = false) const {
         if constexpr (VARIANT == kTopDown) {
-            if (deleteRootImpl(items, size, threshold, check)) deleteUpdate(smemOffset);
+            if (deleteRootImpl(items, size, threshold, check, fair)) deleteUpdate(smemOffset);
         } else {
-            deleteMinBottomUp(items, size, threshold, check, smemOffset);
+            deleteMinBottomUp(items, size, threshold, check, smemOffset, fair);
         }
     }
 
     __device__ __forceinline__ void deleteMinBottomUp(K* items, int& size, K threshold, bool check,
-                                                      int smemOffset) const {
+                                                      int smemOffset, bool fair = false) const {
         K* base = region(smemOffset);
         Op op(this, ctl(base));
         OpCtl* c = op.c;
@@ -1055,7 +1076,10 @@ struct Heap {
         size = 0;
         if (tid == 0) {
             c->w[0] = 0;  // 0: nothing, 1: partial buffer only, 2: root
-            const bool ok = detail::ld_relaxed(&state->err) == 0 && lock(0, 0, BU::INUSE, kSiteLockPartial);
+            const int turn = fair ? takeTurn() : -1;
+            const bool ok =
+                turn != -2 && detail::ld_relaxed(&state->err) == 0 && lock(0, 0, BU::INUSE, kSiteLockPartial);
+            if (turn >= 0) detail::st_release(&state->delServing, turn + 1);
             c->abort = !ok;
             if (ok) {
                 const int bc = detail::ld_relaxed(&state->batchCount);

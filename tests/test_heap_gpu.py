@@ -49,11 +49,12 @@ def _cuda(ghlib):
     yield
 
 
-@pytest.mark.parametrize("i", range(len(golden_cases.meta())))
-def test_golden_replay_single_block(i):
+@pytest.mark.parametrize("which,i", golden_cases.all_ids())
+def test_golden_replay_single_block(which, i):
     """One block replays the reference's operation list; heap memory, counters,
-    deleteRoot sizes and the HEAP_SORT stream equal the reference's run."""
-    c = golden_cases.case(i)
+    deleteRoot sizes and the HEAP_SORT stream equal the reference's run.  Both
+    sets: batch 16-64 and the configurations' batch sizes 256-2048."""
+    c = golden_cases.case(i, which)
     key, B = c["key"], c["batch_size"]
     h = gh.Heap(c["batch_num"], B, key=key, variant="topdown" if c["topdown"] else "bottomup",
                 partial_buffer=c["partial_buffer"])
@@ -230,6 +231,25 @@ def run_heap_sort(key, variant, pb, B, n, dist="uniform", seed=1, chunk=None, gr
 def test_heap_sort_grid(variant, pb, B, logn):
     n = (2**logn + B - 1) // B * B
     got, want = run_heap_sort("u32", variant, pb, B, n, seed=logn * 131 + B)
+    assert np.array_equal(got, want)
+
+
+# The at-scale configurations (batch 256 and 512 x both layouts x with and
+# without the partial buffer, u64 keys, Zipf keys) at 2^24 keys, with the
+# library's default wait limit of 2 s: no wait of a bulk insert or delete may
+# come near it.
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("pb", [True, False])
+@pytest.mark.parametrize("B", [256, 512])
+def test_heap_sort_2e24_default_wait_limit(variant, pb, B):
+    got, want = run_heap_sort("u32", variant, pb, B, 1 << 24, seed=B + 24, chunk=B)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("variant", ["topdown", "bottomup"])
+@pytest.mark.parametrize("key,dist,B", [("u64", "uniform", 1024), ("u32", "zipf", 2048), ("u64", "zipf", 512)])
+def test_heap_sort_2e24_keys_and_zipf(variant, key, dist, B):
+    got, want = run_heap_sort(key, variant, True, B, 1 << 24, dist=dist, seed=B + 7, chunk=B)
     assert np.array_equal(got, want)
 
 
