@@ -413,15 +413,18 @@ def our_arm(args):
     value = job_rate(n, ws, args.steps, total_ms)
     ins_b, del_b = algorithmic_bytes(n, B, s, pb)
     ti, td = statistics.mean(t_ins), statistics.mean(t_del)
-    kern, kb, kt = ("k_delete", del_b, td) if td >= ti else ("k_insert", ins_b, ti)
+    del_kern = "k_delete_owner" if owner else "k_delete"  # the owner launch does all but the last few deletes
+    ins_kern = "k_insert_reserved"  # full batches (chunk = batch_size) into reserved targets
+    kern, kb, kt = (del_kern, del_b, td) if td >= ti else (ins_kern, ins_b, ti)
     peak, peak_kind = peaks()
     achieved = kb / (kt / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 5), "traffic": ncu_traffic(kern, args, pb),
             "kernel": kern, "peak_source": f"{peak_kind} hbm_gbs",
             "algorithmic_bytes": kb, "launch_ms": round(kt, 3),
-            "note": "achieved = closed-form BGPQ node bytes of the launch / its CUDA-event time; frac of measured; "
-                    "traffic = ncu DRAM read+write bytes of one launch of this workload (1 pass), null if not captured"}
+            "note": "achieved = closed-form BGPQ node bytes of the phase / its CUDA-event time (for deletes: the "
+                    "owner-mode launch plus the plain k_delete for the last few nodes); frac of measured; traffic = ncu "
+                    "DRAM read+write bytes of one launch of this kernel on this workload (1 pass), null if not captured"}
     line = {
         "metric": METRIC.format(log2n=args.log2n, key=args.key), "value": round(value, 3), "unit": "M keys/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,

@@ -89,11 +89,11 @@ def test_roofline_traffic_is_the_capture_for_the_exact_workload():
         sys.argv = sys_argv
     with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
         d = json.load(f)
-    e = d["k_delete/bottomup/pb/B2048/u32/uniform/2^28"]
-    assert bench.ncu_traffic("k_delete", a, True) == e["read"] + e["write"]
-    assert bench.ncu_traffic("k_insert", a, True) > 0
-    assert bench.ncu_traffic("k_delete", a, False) is None
+    e = d["k_delete_owner/bottomup/pb/B2048/u32/uniform/2^28"]
+    assert bench.ncu_traffic("k_delete_owner", a, True) == e["read"] + e["write"]
+    assert bench.ncu_traffic("k_insert_reserved", a, True) > 0
+    assert bench.ncu_traffic("k_delete_owner", a, False) is None
     a.log2n = 25
-    assert bench.ncu_traffic("k_delete", a, True) is None
+    assert bench.ncu_traffic("k_delete_owner", a, True) is None
     a.log2n, a.grid = 28, 76
-    assert bench.ncu_traffic("k_delete", a, True) is None
+    assert bench.ncu_traffic("k_delete_owner", a, True) is None
