@@ -60,6 +60,8 @@ _SIGS = {
     "gh_heap_inject_lock": (_I, [_VP, _I, _I]),
     "gh_launch_count": (_LL, []),
     "gh_heap_owner_stats": (_I, [_VP, _VP, _I]),
+    "gh_merge_batches": (_I, [_I, _I, _VP, _VP, _I, _VP, _VP, _I, _VP]),
+    "gh_sort_batch": (_I, [_I, _VP, _I, _VP, _I, _VP]),
     "gh_sort_noalloc": (_I, [_I, _I, _I, _I, _VP, _LL, _VP, _VP]),
     "gh_gen_keys": (_I, [_I, _I, ctypes.c_ulonglong, _LL, _VP, _VP]),
     "gh_rmat_edges": (_I, [_I, _LL, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong,

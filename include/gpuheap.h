@@ -375,6 +375,22 @@ gh_status gh_serve_info(gh_server* s, long long* used_bytes, long long* free_byt
 gh_status gh_gen_grid(int width, int height, unsigned long long seed, int obstacle_per_mille, unsigned char* out_host,
                       int threads);
 
+/* The heap's block primitives on their own, one block on `stream`, for tests
+ * and tuning: no Heap<K> involved.  The reference tests its counterparts
+ * (imergePath, ibitonicSort, heap/heaputil.cuh:23-47,99-158) with
+ * local_test/merge_path; these are not entry points there.
+ * gh_merge_batches: a_dev and b_dev each hold n sorted keys (n a power of
+ * two in [16, 8192]); the n smallest of both go to lo_dev, the n largest to
+ * hi_dev, in order.  method 0: the merge of every insert and sift step (merge
+ * path, 2n / threads keys per thread, 1..16); method 1: the owner-mode
+ * delete's warp-window merge (windows of 1024 four-byte or 512 eight-byte
+ * keys, so 2n at least one window).  gh_sort_batch: sorts in_dev[0, n) (n a
+ * power of two in [2, 8192]) into out_dev with the insert batch's bitonic
+ * network.  threads: a power of two in [32, 1024]. */
+gh_status gh_merge_batches(int key_kind, int method, const void* a_dev, const void* b_dev, int n, void* lo_dev,
+                           void* hi_dev, int threads, void* stream);
+gh_status gh_sort_batch(int key_kind, const void* in_dev, int n, void* out_dev, int threads, void* stream);
+
 /* Number of kernels this library has launched since it was loaded. */
 long long gh_launch_count(void);
 

@@ -88,3 +88,21 @@ def test_newer_entry_points_reject_bad_arguments(ghlib):
     assert ghlib.gh_serve_set_blocks(None, 1 << 15, 24, 1 << 18, 8) == 1
     cnt = (ctypes.c_int * 3)(0, 0, 0)
     assert ghlib.gh_heap_restore(None, ctypes.byref(t), cnt) == 1
+
+
+def test_primitive_and_owner_entry_points_reject_bad_arguments(ghlib):
+    """The block-primitive entry points, the owner-mode depth setter and the
+    owner counters refuse bad shapes or a missing handle with GH_ERR_INVALID
+    before any device work."""
+    p = ctypes.c_void_p(16)  # never dereferenced: the checks come first
+    assert ghlib.gh_merge_batches(0, 0, p, p, 100, p, p, 128, None) == 1      # n not a power of two
+    assert ghlib.gh_merge_batches(0, 0, p, p, 2048, p, p, 32, None) == 1      # 128 keys per thread
+    assert ghlib.gh_merge_batches(0, 1, p, p, 256, p, p, 256, None) == 1      # below one 1024-key window
+    assert ghlib.gh_merge_batches(0, 2, p, p, 256, p, p, 256, None) == 1      # no such method
+    assert ghlib.gh_merge_batches(3, 0, p, p, 256, p, p, 256, None) == 1      # no such key kind
+    assert ghlib.gh_merge_batches(0, 0, None, p, 256, p, p, 256, None) == 1
+    assert ghlib.gh_sort_batch(0, p, 100, p, 128, None) == 1
+    assert ghlib.gh_sort_batch(0, p, 256, p, 48, None) == 1
+    assert ghlib.gh_heap_set_owner_depth(None, 2) == 1
+    out = (ctypes.c_ulonglong * 4)()
+    assert ghlib.gh_heap_owner_stats(None, out, 4) == 1
