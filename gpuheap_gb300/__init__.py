@@ -81,6 +81,7 @@ _SIGS = {
     "gh_batch_add_knapsack": (_I, [_VP, _I, _VP, _VP, _LL, ctypes.POINTER(_I)]),
     "gh_batch_build": (_I, [_VP, _VP]),
     "gh_batch_run": (_I, [_VP, _I, _VP]),
+    "gh_batch_plain_times": (_I, [_VP, _VP]),
     "gh_batch_results": (_I, [_VP, _VP, _VP, _VP, _VP]),
     "gh_batch_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                            ctypes.POINTER(_LL)]),

@@ -106,6 +106,12 @@ class Batch:
             _check(rc, "batch_results")
         return res, st, stats
 
+    def plain_times(self):
+        """Milliseconds of each instance's own launch in the last plain run."""
+        out = np.zeros(len(self.kinds), np.float32)
+        _check(lib().gh_batch_plain_times(self._h, out.ctypes.data), "batch_plain_times")
+        return out
+
     def knapsack_switches(self, stream=None):
         """Heap/FIFO switches per instance in the last run (knapsack, order "switch")."""
         out = np.zeros(len(self.kinds), np.int32)

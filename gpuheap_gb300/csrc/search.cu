@@ -76,6 +76,7 @@ struct gh_batch {
     long long graphLaunches = 0;
     int grid = 0;  // blocks of the persistent launch
     bool built = false;
+    std::vector<cudaEvent_t> plainEv;  // one-launch-per-instance runs: an event before each launch and one after
 };
 
 namespace {
@@ -139,9 +140,19 @@ gh_status gh_batch_create(gh_batch** out, int batch_size, int variant, int block
 
 gh_status gh_batch_destroy(gh_batch* b) {
     if (!b) return GH_ERR_INVALID;
+    for (cudaEvent_t e : b->plainEv) cudaEventDestroy(e);
     free_device(b);
     if (b->graphStream) cudaStreamDestroy(b->graphStream);
     delete b;
+    return GH_OK;
+}
+
+gh_status gh_batch_plain_times(gh_batch* b, float* ms_out) {
+    const int count = b ? static_cast<int>(b->host.size()) : 0;
+    if (!b || !ms_out || static_cast<int>(b->plainEv.size()) < count + 1 || count == 0) return GH_ERR_INVALID;
+    if (cudaEventSynchronize(b->plainEv[count]) != cudaSuccess) return GH_ERR_CUDA;
+    for (int i = 0; i < count; ++i)
+        if (cudaEventElapsedTime(&ms_out[i], b->plainEv[i], b->plainEv[i + 1]) != cudaSuccess) return GH_ERR_CUDA;
     return GH_OK;
 }
 
@@ -456,10 +467,19 @@ gh_status reset_and_run(gh_batch* b, int mode, cudaStream_t s) {
     gh::impl::count_launch();
     if (cudaGetLastError() != cudaSuccess) return GH_ERR_CUDA;
     if (mode == GH_BATCH_PLAIN) {
+        // an event before each instance's launch and one after the last, so
+        // that gh_batch_plain_times can give every instance its own time
+        while (static_cast<int>(b->plainEv.size()) < count + 1) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return GH_ERR_CUDA;
+            b->plainEv.push_back(e);
+        }
         for (int i = 0; i < count; ++i) {
+            if (cudaEventRecord(b->plainEv[i], s) != cudaSuccess) return GH_ERR_CUDA;
             if (launch(b, b->tasks + b->segOff[i], b->segLen[i], b->next + 1 + i, b->segLen[i], s) != cudaSuccess)
                 return GH_ERR_CUDA;
         }
+        if (cudaEventRecord(b->plainEv[count], s) != cudaSuccess) return GH_ERR_CUDA;
     } else {
         if (launch(b, b->tasks, b->ntasks, b->next, b->grid, s) != cudaSuccess) return GH_ERR_CUDA;
     }

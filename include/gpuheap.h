@@ -300,6 +300,11 @@ gh_status gh_batch_build(gh_batch* b, void* stream);
  * the first call; GH_BATCH_PLAIN one launch per instance, back to back (the
  * reference's way).  Asynchronous. */
 gh_status gh_batch_run(gh_batch* b, int mode, void* stream);
+/* Milliseconds of each instance's own launch in the last GH_BATCH_PLAIN run
+ * (events around every launch; waits for the run).  GH_ERR_INVALID before
+ * any plain run.  No counterpart in the reference (its drivers time whole
+ * runs). */
+gh_status gh_batch_plain_times(gh_batch* b, float* ms_out);
 /* Synchronizes and copies out per-instance results (may be NULL), status
  * (gh_status per instance, may be NULL) and stats (3 per instance: keys
  * taken, keys expanded, keys inserted; may be NULL).  Returns the first
