@@ -57,7 +57,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--timeout", type=float, default=2.0,
-                   help="device wait limit in seconds (raise it under a profiler)")
+                   help="heap-sort and FIFO: device wait limit in seconds (raise it under a profiler)")
+    p.add_argument("--search-timeout", type=float, default=20.0,
+                   help="SSSP and batched searches: device wait limit in seconds (a search block can idle for as "
+                        "long as the largest instance runs)")
     p.add_argument("--workload", choices=["heapsort", "sssp", "batched", "served", "fifo"], default="heapsort",
                    help="heapsort: the plain heap-sort line (default); sssp: SSSP with the queue; "
                         "batched: grid A* + knapsack searches in one persistent launch vs per-instance launches; "
@@ -497,7 +500,7 @@ def sssp_arm(args):
     heap = gs.make_heap(g, batch_size=args.batch, variant=args.variant)
     if args.grid:
         heap.set_grid(args.grid)
-    heap.set_timeout(args.timeout)
+    heap.set_timeout(args.search_timeout)
     info = heap.info()
     for i in range(args.warmup):
         gs.sssp(heap, g, int(srcs[i % len(srcs)]))
@@ -598,7 +601,7 @@ def batched_arm(args):
         cfg = gb.autotune(inst)
     b = gb.Batch(inst, batch_size=cfg["batch_size"], variant=cfg["variant"],
                  astar_cells_per_block=cfg["astar_cells_per_block"], astar_max_blocks=cfg.get("astar_max_blocks", 8),
-                 timeout=args.timeout, knapsack_order=args.knapsack_order)
+                 timeout=args.search_timeout, knapsack_order=args.knapsack_order)
     info = b.info()
     stream = torch.cuda.current_stream()
     for _ in range(max(args.warmup, 1)):
@@ -630,7 +633,7 @@ def batched_arm(args):
             pb = b if name == "batched tuning" else gb.Batch(
                 inst, batch_size=c["batch_size"], variant=c["variant"],
                 astar_cells_per_block=c["astar_cells_per_block"], astar_max_blocks=c["astar_max_blocks"],
-                timeout=args.timeout, knapsack_order=args.knapsack_order)
+                timeout=args.search_timeout, knapsack_order=args.knapsack_order)
             runs = []
             for _ in range(args.plain_steps):
                 pb.run("plain", stream)
