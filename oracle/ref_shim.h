@@ -62,6 +62,8 @@ inline int atomicCAS(int* a, int cmp, int val) {
     return old;
 }
 inline int atomicAdd(int* a, int v) { int old = *a; *a += v; return old; }
+inline int atomicExch(int* a, int v) { int old = *a; *a = v; return old; }
+inline void __threadfence() {}
 inline int atomicSub(int* a, int v) { int old = *a; *a -= v; return old; }
 inline int atomicMax(int* a, int v) {
     int old = *a;

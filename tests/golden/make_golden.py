@@ -9,12 +9,15 @@ phase and at the end.  These vectors pin both the oracle restatement (CPU
 tests) and the CUDA path (GPU tests, one thread block, where the heap is
 deterministic).
 
-Two sets: `small` (bgpq_ref_cases.npz, batch 16-64, every key type and
-scenario) and `large` (bgpq_ref_cases_large.npz, batch 256-2048, the batch
-sizes of the heap-sort configurations).
+Three sets: `small` (bgpq_ref_cases.npz, batch 16-64, every key type and
+scenario), `large` (bgpq_ref_cases_large.npz, batch 256-2048, the batch
+sizes of the heap-sort configurations) and `retrieve`
+(retrieve_ref_cases.npz: insert / retrieve sequences through the reference's
+retrieving heap, applications/sssp_longfei_new/heap.cuh, pinning the runs
+that `retrieve` returns).
 
 Usage (needs the reference tree; not run by the tests):
-    make -C oracle ref REF=<reference tree> && python tests/golden/make_golden.py [small] [large]
+    make -C oracle ref REF=<reference tree> && python tests/golden/make_golden.py [small] [large] [retrieve]
 """
 import ctypes
 import json
@@ -176,16 +179,72 @@ def large_cases():
             yield variant, kind, scenario, B, seed, rng, nb
 
 
-SETS = {"small": (small_cases, "bgpq_ref_cases.npz"), "large": (large_cases, "bgpq_ref_cases_large.npz")}
+def run_retrieve_case(ref, kind, B, seed, rng, n_ops):
+    """One seeded sequence of insert(count) / retrieve(size) calls through
+    the reference's retrieving heap (applications/sssp_longfei_new/heap.cuh);
+    returns (arrays, meta).  ops: positive = insert that many keys, negative
+    = retrieve -op keys; `taken` = each retrieve's count, `runs` = the
+    retrieved keys, concatenated."""
+    dt, ct, lim = TYPES[kind]
+    bn = 512
+    f = lambda name, res=ctypes.c_int: _fn_rr(ref, kind, name, res)
+    create = f("create", VP)
+    create.argtypes = [ctypes.c_int, ctypes.c_int, ct]
+    h = create(bn, B, lim)
+    ops, keys, taken, runs = [], [], [], []
+    held = 0
+    ties = seed % 3 == 0
+    for _ in range(n_ops):
+        if rng.random() < 0.55 and held + B < (bn - 8) * B:
+            c = int(rng.integers(1, B + 1))
+            ks = keys_for(rng, kind, c, False, ties=ties)
+            assert f("insert")(VP(h), VP(np.ascontiguousarray(ks).ctypes.data), c) == 0
+            ops.append(c)
+            keys.append(ks)
+            held += c
+        else:
+            size = int(rng.integers(1, B + 1)) if rng.random() < 0.8 else B
+            out = np.zeros(B, dt)
+            sz = ctypes.c_int(size)
+            assert f("retrieve")(VP(h), VP(out.ctypes.data), ctypes.byref(sz)) == 0
+            ops.append(-size)
+            taken.append(sz.value)
+            runs.append(out[:sz.value].copy())
+            held -= sz.value
+    f("destroy", None)(VP(h))
+    arrays = dict(ops=np.asarray(ops, np.int32), keys=np.concatenate(keys) if keys else np.zeros(0, dt),
+                  taken=np.asarray(taken, np.int32), runs=np.concatenate(runs) if runs else np.zeros(0, dt))
+    meta = dict(key=kind, batch_size=B, seed=seed, ties=ties)
+    return arrays, meta
+
+
+def retrieve_cases():
+    """12 sequences of inserts and retrievals: {u32, u64} x batch {16, 64,
+    256} x two seeds (every third seed draws keys from ~40 values)."""
+    for kind in ("u32", "u64"):
+        for B in (16, 64, 256):
+            for k in range(2):
+                seed = 9000 + 31 * B + 7 * k + (0 if kind == "u32" else 1)
+                yield kind, B, seed, np.random.default_rng(seed), 160
+
+
+def _fn_rr(lib, kind, name, res):
+    fn = getattr(lib, f"rr_{kind}_{name}")
+    fn.restype = res
+    return fn
+
+
+SETS = {"small": (small_cases, "bgpq_ref_cases.npz"), "large": (large_cases, "bgpq_ref_cases_large.npz"),
+        "retrieve": (retrieve_cases, "retrieve_ref_cases.npz")}
 
 
 def main(argv):
     ref = ctypes.CDLL(LIB)
-    for name in (argv or ["small", "large"]):
+    for name in (argv or ["small", "large", "retrieve"]):
         gen, fname = SETS[name]
         arrays, meta = {}, []
         for case, params in enumerate(gen()):
-            a, m = run_case(ref, *params)
+            a, m = (run_retrieve_case if name == "retrieve" else run_case)(ref, *params)
             arrays.update({f"c{case}_{k}": v for k, v in a.items()})
             meta.append(dict(case=case, **m))
         arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)

@@ -1,6 +1,7 @@
 """Loader for the golden vectors made by tests/golden/make_golden.py from the
 reference's own heap headers: `small` (bgpq_ref_cases.npz, batch 16-64) and
-`large` (bgpq_ref_cases_large.npz, batch 256-2048)."""
+`large` (bgpq_ref_cases_large.npz, batch 256-2048); and the insert/retrieve
+sequences of the reference's retrieving heap (retrieve_ref_cases.npz)."""
 import json
 import os
 
@@ -33,3 +34,26 @@ def case(i, which="small"):
 def all_ids():
     """(set, index) of every golden case, for parametrising."""
     return [(w, i) for w in FILES for i in range(len(meta(w)))]
+
+
+RETRIEVE_FILE = "retrieve_ref_cases.npz"
+
+
+def retrieve_meta():
+    return json.loads(bytes(_retrieve_data()["meta"]).decode())
+
+
+def _retrieve_data():
+    if "retrieve" not in _data:
+        _data["retrieve"] = np.load(os.path.join(_DIR, RETRIEVE_FILE))
+    return _data["retrieve"]
+
+
+def retrieve_case(i):
+    """ops (positive: insert that many of `keys` in order; negative: retrieve
+    -op keys), taken (each retrieve's count), runs (retrieved keys, joined)."""
+    d = _retrieve_data()
+    p = f"c{i}_"
+    out = {k[len(p):]: d[k] for k in d.files if k.startswith(p)}
+    out.update(retrieve_meta()[i])
+    return out
