@@ -76,6 +76,11 @@ def parse():
     p.add_argument("--plain-queries", type=int, default=48, help="served: queries run alone for the baseline")
     p.add_argument("--batches-per-step", type=int, default=32, help="served: batches a block takes per query per step")
     p.add_argument("--served-batch", type=int, default=1024, help="served: batch size of every query's heap")
+    p.add_argument("--served-mode", choices=["device", "host"], default="device",
+                   help="served: the device-resident request loop, or one host step per launch")
+    p.add_argument("--idle-ms", type=int, default=100, help="served, device loop: idle limit of its launch")
+    p.add_argument("--no-host-steps", action="store_true",
+                   help="served, device loop: skip the host-step comparison at the same rates")
     p.add_argument("--instances", type=int, default=1024, help="batched: searches per step")
     p.add_argument("--plain-steps", type=int, default=1, help="batched: timed runs of the per-instance launches")
     p.add_argument("--no-tune", action="store_true", help="batched: skip the autotuner (batch 256, bottom-up)")
@@ -745,10 +750,13 @@ def served_cpu_leg(graphs_host, maps_host, queries, threads):
 
 def served_arm(args):
     """Per offered rate: `queries` seeded queries arrive by a Poisson process
-    and go through the server (admission by free memory, one launch per step
-    over every admitted query); latency = finish - arrival.  The baseline
-    runs a sample of the same mix one query at a time, each alone on the
-    GPU, in one launch, until it finishes."""
+    and go through the server -- by default its device-resident request loop
+    (admission by free memory, setup, search, collection and freeing inside
+    one persistent launch; the host posts requests and reads completions),
+    then, for comparison, its host steps (one launch and one synchronization
+    per step); latency = completion seen by the host - arrival.  The
+    baseline runs a sample of the same mix one query at a time, each alone
+    on the GPU, in one launch, until it finishes."""
     import numpy as np
     import torch
 
@@ -775,24 +783,40 @@ def served_arm(args):
         return s
 
     rates = [float(r) for r in args.rates.split(",")]
-    srv = server(max_slots=256, batch_size=args.served_batch, batches_per_step=args.batches_per_step)
-    warm = served_queries(graphs, maps, 8, args.seed + 99)
-    gs.run_stream(srv, warm, np.zeros(len(warm)))
-    per_rate, l0 = [], gh.launch_count()
-    with ClockSampler(local) as clk:
+    device_loop = args.served_mode == "device"
+
+    def serve_rates(resident):
+        """Every offered rate through one server: the device-resident loop
+        (resident) or host steps.  Returns (per-rate records, launches)."""
+        srv = server(max_slots=256, batch_size=args.served_batch, batches_per_step=args.batches_per_step)
+        if resident:
+            srv.start(idle_ms=args.idle_ms)
+        warm = served_queries(graphs, maps, 8, args.seed + 99)
+        gs.run_stream(srv, warm, np.zeros(len(warm)), resident=resident)
+        if resident:  # the loop's launch leaves; the first poll of the timed streams launches it again
+            srv.stop()
+            srv.start(idle_ms=args.idle_ms)
+        out, l0 = [], gh.launch_count()
         for i, rate in enumerate(rates):
             qs = served_queries(graphs, maps, args.queries, args.seed + i)
             arr = gs.poisson_arrivals(len(qs), rate, args.seed + 1000 + i)
-            lat, res, makespan, steps = gs.run_stream(srv, qs, arr)
+            lat, res, makespan, steps = gs.run_stream(srv, qs, arr, resident=resident)
             bad = [r for r in res if r[0] != gs.FINISHED]
             if bad:
                 raise SystemExit(f"bench: {len(bad)} served queries failed at {rate} req/s")
-            per_rate.append({"offered_per_s": rate, "queries": len(qs), "served_per_s": round(len(qs) / makespan, 2),
-                             "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
-                             "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
-                             "makespan_s": round(makespan, 3), "steps": steps})
-    launches = gh.launch_count() - l0
-    srv.close()
+            out.append({"offered_per_s": rate, "queries": len(qs), "served_per_s": round(len(qs) / makespan, 2),
+                        "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
+                        "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2),
+                        "makespan_s": round(makespan, 3), ("polls" if resident else "steps"): steps})
+        launches = gh.launch_count() - l0
+        if resident:
+            out[-1]["loop_launches"] = srv.info()["steps"]
+        srv.close()
+        return out, launches
+
+    with ClockSampler(local) as clk:
+        per_rate, launches = serve_rates(device_loop)
+    host_rates = serve_rates(False)[0] if device_loop and not args.no_host_steps else None
     # baseline: a sample of the same mix, one query at a time, each alone on the
     # GPU in the configuration that suits it best: SSSP through the standalone
     # kernel (gh_sssp, batch 2048 on 24 blocks), A* alone in the engine
@@ -826,7 +850,9 @@ def served_arm(args):
     plain_qps = len(plain_q) / float(secs.sum())
     mix = served_queries(graphs, maps, args.plain_queries, args.seed + 777)
     srv = server(max_slots=256, batch_size=args.served_batch, batches_per_step=args.batches_per_step)
-    _, res_mix, _, _ = gs.run_stream(srv, mix, np.zeros(len(mix)))
+    if device_loop:
+        srv.start(idle_ms=args.idle_ms)
+    _, res_mix, _, _ = gs.run_stream(srv, mix, np.zeros(len(mix)), resident=device_loop)
     srv.close()
     same = [(r[1], r[2]) for r in res_alone] == [(r[1], r[2]) for r in res_mix]
     top = per_rate[-1]
@@ -840,12 +866,17 @@ def served_arm(args):
                                f"(20% obstacles, costs 1-9) between random cells; size class k weighted 4^-k",
                    "batch_size": args.served_batch, "variant": "bottomup", "max_slots": 256,
                    "batches_per_step": args.batches_per_step, "setup_s": round(setup_s, 2),
+                   "loop": ("device-resident request loop (pinned request / completion rings, one persistent "
+                            f"launch, idle exit after {args.idle_ms} ms)") if device_loop
+                           else "host steps (one launch and one synchronization per step)",
                    "parallelism": f"replicas x{ws}"},
         "rates": per_rate, "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
         "plain_per_s": round(plain_qps, 2), "served_vs_plain": round(top["served_per_s"] / plain_qps, 2),
         "alone_equals_mix": f"{len(plain_q)} queries: {'identical' if same else 'DIFFERENT'} results alone and in the mix",
         "gpu_launches": launches, "clocks": clk.summary(),
     }
+    if host_rates is not None:
+        line["host_step_rates"] = host_rates
     if not same:
         raise SystemExit("bench: served results differ between alone and in the mix")
     if rank == 0 and not args.no_cpu:

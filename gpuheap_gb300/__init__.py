@@ -97,6 +97,9 @@ _SIGS = {
                              ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(_LL)]),
     "gh_serve_finished": (_I, [_VP, _VP, _I, ctypes.POINTER(_I)]),
     "gh_serve_info": (_I, [_VP, ctypes.POINTER(_LL), ctypes.POINTER(_LL), ctypes.POINTER(_I), ctypes.POINTER(_LL)]),
+    "gh_serve_start": (_I, [_VP, _I]),
+    "gh_serve_poll": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "gh_serve_stop": (_I, [_VP]),
     "gh_fifo_create": (_I, [ctypes.POINTER(_VP), _I, _LL]),
     "gh_fifo_destroy": (_I, [_VP]),
     "gh_fifo_reset": (_I, [_VP, _VP]),

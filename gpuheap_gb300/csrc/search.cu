@@ -38,8 +38,11 @@
 #include <vector>
 
 #include "gpuheap.h"
-#include "search_kernels.cuh"
+#include "heap_kernels.cuh"
+#include "search_common.cuh"
 #include "trace.cuh"
+
+using namespace gh::search;
 
 // ---------------------------------------------------------------------- host side
 struct HostInst {
@@ -87,7 +90,7 @@ SearchConfig config_of(const gh_batch* b) {
 int threads_for(const gh_batch* b) { return search_threads(config_of(b)); }
 int resident_blocks(const gh_batch* b) { return search_resident_blocks(config_of(b)); }
 cudaError_t launch(const gh_batch* b, const int* tasks, int ntasks, int* next, int grid, cudaStream_t s) {
-    return search_launch(config_of(b), b->insts, tasks, ntasks, next, grid, s, 0);
+    return search_launch(config_of(b), SearchArgs{b->insts, tasks, ntasks, next, 0, nullptr}, grid, s);
 }
 
 void free_device(gh_batch* b) {
@@ -461,11 +464,9 @@ namespace {
 gh_status reset_and_run(gh_batch* b, int mode, cudaStream_t s) {
     const int count = static_cast<int>(b->host.size());
     if (cudaMemsetAsync(b->next, 0, static_cast<size_t>(count + 1) * 4, s) != cudaSuccess) return GH_ERR_CUDA;
-    k_search_fill<<<dim3(8, count), 256, 0, s>>>(b->insts, nullptr, b->batchSize);
-    gh::impl::count_launch();
-    k_search_seed<<<(count + 127) / 128, 128, 0, s>>>(b->insts, nullptr, count);
-    gh::impl::count_launch();
-    if (cudaGetLastError() != cudaSuccess) return GH_ERR_CUDA;
+    if (search_fill(b->insts, nullptr, count, b->batchSize, s) != cudaSuccess ||
+        search_seed(b->insts, nullptr, count, s) != cudaSuccess)
+        return GH_ERR_CUDA;
     if (mode == GH_BATCH_PLAIN) {
         // an event before each instance's launch and one after the last, so
         // that gh_batch_plain_times can give every instance its own time
@@ -483,9 +484,7 @@ gh_status reset_and_run(gh_batch* b, int mode, cudaStream_t s) {
     } else {
         if (launch(b, b->tasks, b->ntasks, b->next, b->grid, s) != cudaSuccess) return GH_ERR_CUDA;
     }
-    k_search_collect<<<count, 256, 0, s>>>(b->insts, nullptr, 1, b->batchSize);
-    gh::impl::count_launch();
-    return cudaGetLastError() == cudaSuccess ? GH_OK : GH_ERR_CUDA;
+    return search_collect(b->insts, nullptr, count, 1, b->batchSize, s) == cudaSuccess ? GH_OK : GH_ERR_CUDA;
 }
 
 }  // namespace

@@ -42,15 +42,12 @@
 #include "gpuheap.h"
 #include "gpuheap_fifo.cuh"
 #include "heap_launch.cuh"
+#include "search_common.cuh"
 #include "sssp_relax.cuh"
 #include "worklist.cuh"
 
-namespace {
-
-using u64 = unsigned long long;
-constexpr int kMaxKnapItems = 1024;
-constexpr int kMaxSearchThreads = 512;  // 128 registers per thread
-constexpr int kSlotBits = 20;            // knapsack key: pool slot bits below the level
+namespace gh {
+namespace search {
 
 __device__ __forceinline__ u64 knap_key(long long bound, int level, int slot) {
     return (static_cast<u64>(static_cast<unsigned>(INT_MAX - static_cast<int>(bound))) << 32) |
@@ -58,50 +55,6 @@ __device__ __forceinline__ u64 knap_key(long long bound, int level, int slot) {
 }
 
 // One instance, as the kernels see it (device array).
-struct alignas(16) Inst {
-    int kind;      // GH_SEARCH_ASTAR / GH_SEARCH_KNAPSACK / GH_SEARCH_SSSP
-    int blocks;    // blocks that join it
-    int batchNum;  // heap nodes
-    int stop;      // set when an instance-level failure ends the search
-    u64* items;
-    int* status;
-    gh::HeapState* state;
-    // A*: grid, start and goal cell; SSSP: g holds the distances
-    int width, height;
-    const unsigned char* cost;
-    unsigned* g;
-    int start, goal;
-    // SSSP: CSR graph with nv vertices, source vertex
-    int nv, source;
-    const long long* rowptr;
-    const int* col;
-    const unsigned* wt;
-    // knapsack: ratio-ordered items and exclusive prefix sums
-    int n, poolCap;
-    long long cap;
-    const int* w;
-    const int* p;
-    const long long* W;
-    const long long* P;
-    int4* pool;  // (level, profit, weight, 0)
-    int* freeList;
-    int freeTop, bump;  // pool allocator, owned by the instance's single block
-    // result and statistics
-    int incumbent;  // A*: best goal cost (as unsigned); knapsack: best profit
-    int failed;     // gh_status of a failure, 0 if none
-    unsigned long long pops, expanded, inserted;
-    int greedy;  // knapsack: profit of the greedy fill (first incumbent)
-    int done;    // the search has finished (heap empty, no block inside)
-    unsigned long long reached, distSum;  // SSSP: reachable vertices, sum of their distances
-    // knapsack FIFO / switch models (ring == NULL: heap only)
-    u64* ring;                  // ringCap keys, a power of two
-    gh::FifoState* fifo;
-    unsigned long long ringCap;
-    int order;                  // GH_KNAP_HEAP / GH_KNAP_FIFO / GH_KNAP_SWITCH
-    int switchCounter;          // batches in a row that trigger a switch
-    int mode;                   // structure in use: 0 heap, 1 FIFO
-    int switches;               // mode changes so far
-};
 
 // Prune thresholds (the app_t_val of deleteRoot, artifacts/astar/BGPQ_B/
 // heap.cuh:260-289): keys at or above them cannot improve the incumbent, so
@@ -124,8 +77,8 @@ struct KnapThreshold {
 };
 
 __device__ __forceinline__ u64 prune_threshold(const Inst* in) {
-    if (in->kind == GH_SEARCH_ASTAR) return static_cast<u64>(static_cast<unsigned>(in->incumbent)) << 32;
-    if (in->kind == GH_SEARCH_KNAPSACK) return static_cast<u64>(static_cast<unsigned>(INT_MAX - in->incumbent)) << 32;
+    if (in->kind == GH_SEARCH_ASTAR) return static_cast<u64>(static_cast<unsigned>(__ldcg(&in->incumbent))) << 32;
+    if (in->kind == GH_SEARCH_KNAPSACK) return static_cast<u64>(static_cast<unsigned>(INT_MAX - __ldcg(&in->incumbent))) << 32;
     return ~0ull;  // SSSP relaxes every key
 }
 
@@ -153,20 +106,21 @@ __device__ __forceinline__ long long knap_bound(const long long* W, const long l
     return bound;
 }
 
-// Reset of the listed instances' arrays (ids == NULL: the first gridDim.y):
-// heap nodes to init keys, lock words to AVAIL, A* and SSSP distances to
-// infinity.  blockIdx.y = instance, blockIdx.x = slice.
-__global__ void k_search_fill(Inst* insts, const int* ids, int B) {
-    Inst* in = insts + (ids ? ids[blockIdx.y] : static_cast<int>(blockIdx.y));
-    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
-    const size_t first = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const size_t keys = static_cast<size_t>(in->batchNum + 1) * B;
-    for (size_t q = first; q < keys; q += stride) in->items[q] = ~0ull;
+// Reset of one instance's arrays: heap nodes to init keys, lock words to
+// AVAIL, A* and SSSP distances to infinity, FIFO counters to zero.  Thread
+// `first` of `stride` threads (the threads of several blocks, or of one).
+__device__ inline void fill_instance(const Inst* in, int B, size_t first, size_t stride) {
+    // nodes: (batchNum + 1) * B keys, an even count from a 256-byte aligned base
+    const size_t pairs = static_cast<size_t>(in->batchNum + 1) * B / 2;
+    ulonglong2* items = reinterpret_cast<ulonglong2*>(in->items);
+    for (size_t q = first; q < pairs; q += stride) items[q] = make_ulonglong2(~0ull, ~0ull);
     for (size_t q = first; q < static_cast<size_t>(in->batchNum) + 2; q += stride) in->status[q] = 0;
     if (in->kind == GH_SEARCH_ASTAR || in->kind == GH_SEARCH_SSSP) {
         const size_t cells = in->kind == GH_SEARCH_ASTAR ? static_cast<size_t>(in->width) * in->height
                                                          : static_cast<size_t>(in->nv);
-        for (size_t q = first; q < cells; q += stride) in->g[q] = 0xffffffffu;
+        uint4* g4 = reinterpret_cast<uint4*>(in->g);  // 256-byte aligned base
+        for (size_t q = first; q < cells / 4; q += stride) g4[q] = make_uint4(~0u, ~0u, ~0u, ~0u);
+        for (size_t q = cells / 4 * 4 + first; q < cells; q += stride) in->g[q] = 0xffffffffu;
     }
     if (in->fifo) {
         unsigned long long* w = reinterpret_cast<unsigned long long*>(in->fifo);
@@ -174,19 +128,16 @@ __global__ void k_search_fill(Inst* insts, const int* ids, int B) {
     }
 }
 
-// Counters, incumbent and the seed key in the partial buffer (after the
-// fill), for the listed instances (ids == NULL: the first `count`).
-__global__ void k_search_seed(Inst* insts, const int* ids, int count) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        Inst* in = insts + (ids ? ids[i] : i);
+// Counters, incumbent and the seed key in the partial buffer of one
+// instance, after its fill (one thread).
+__device__ inline void seed_instance(Inst* in) {
+    {
         gh::HeapState* st = in->state;
-        st->batchCount = 0;
-        st->deleteCount = 0;
+        // every counter, ticket and error word to zero: the block may have
+        // held another instance's data before
+        int* words = reinterpret_cast<int*>(st);
+        for (int q = 0; q < static_cast<int>(sizeof(gh::HeapState) / 4); ++q) words[q] = 0;
         st->outLimit = INT_MAX;
-        st->insTicket = 0;
-        st->err = st->errOp = st->errNode = st->errState = 0;
-        st->busy = 0;
-        for (int q = 0; q < 8; ++q) st->appStats[q] = 0;
         in->stop = 0;
         in->failed = 0;
         in->done = 0;
@@ -234,17 +185,6 @@ __global__ void k_search_seed(Inst* insts, const int* ids, int count) {
         }
     }
 }
-
-// Shared memory of a search block, ahead of the heap's region.
-struct SearchSmem {
-    static __host__ __device__ size_t emitKeys(int B, int T) { return static_cast<size_t>(B) + 4 * static_cast<size_t>(T); }
-    static __host__ __device__ size_t bytes(int B, int T) {
-        const size_t keys = (static_cast<size_t>(B) + emitKeys(B, T)) * 8;
-        const size_t knap = static_cast<size_t>(kMaxKnapItems + 1) * 16 + static_cast<size_t>(kMaxKnapItems) * 8 +
-                            static_cast<size_t>(B) * 16;
-        return (keys + knap + 64 + 15) / 16 * 16;
-    }
-};
 
 template <typename H>
 __device__ __forceinline__ void flush_full(const H& heap, u64* emit, int* cnt, int B, int heapOff, unsigned long long& inserted) {
@@ -339,7 +279,7 @@ __device__ void fifo_to_heap(const H& heap, const gh::Fifo<u64>& f, u64* batch, 
 }
 
 template <typename H>
-__device__ void run_astar(const H& heap, Inst* in, unsigned char* smem, int heapOff, int maxBatches) {
+__device__ bool run_astar(const H& heap, Inst* in, unsigned char* smem, int heapOff, int maxBatches) {
     const int B = heap.batchSize, T = blockDim.x, tid = threadIdx.x;
     u64* batch = reinterpret_cast<u64*>(smem);
     u64* emit = batch + B;
@@ -354,8 +294,9 @@ __device__ void run_astar(const H& heap, Inst* in, unsigned char* smem, int heap
     if (tid == 0) ctl[1] = 0;
     __syncthreads();
     const AstarThreshold prune{inc};
+    bool over = true;  // false: the batch budget ran out, the search goes on
     for (;;) {
-        if (maxBatches && batches++ == maxBatches) break;
+        if (maxBatches && batches++ == maxBatches) { over = false; break; }
         if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
         int size = 0;
         heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap), heapOff);
@@ -403,10 +344,11 @@ __device__ void run_astar(const H& heap, Inst* in, unsigned char* smem, int heap
         atomicAdd(&in->inserted, inserted);
     }
     atomicAdd(&in->expanded, expanded);
+    return over;
 }
 
 template <typename H>
-__device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int heapOff, int maxBatches) {
+__device__ bool run_knapsack(const H& heap, Inst* in, unsigned char* smem, int heapOff, int maxBatches) {
     const int B = heap.batchSize, T = blockDim.x, tid = threadIdx.x;
     u64* batch = reinterpret_cast<u64*>(smem);
     u64* emit = batch + B;
@@ -433,8 +375,9 @@ __device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int h
     int mode = in->mode;               // block-uniform: 0 heap, 1 FIFO
     int counter = 0, prevBest = 0;     // switch model, thread 0
     if (tid == 0) prevBest = __ldcg(best);
+    bool over = true;  // false: the batch budget ran out, the search goes on
     for (;;) {
-        if (maxBatches && batches++ == maxBatches) break;
+        if (maxBatches && batches++ == maxBatches) { over = false; break; }
         int size = 0;
         if (mode == 0) {
             if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
@@ -535,12 +478,13 @@ __device__ void run_knapsack(const H& heap, Inst* in, unsigned char* smem, int h
         atomicAdd(&in->inserted, inserted);
     }
     atomicAdd(&in->expanded, expanded);
+    return over;
 }
 
 // SSSP from the instance's source: the label-correcting loop of the
 // standalone SSSP kernel, one expansion step per taken batch.
 template <typename H>
-__device__ void run_sssp(const H& heap, Inst* in, unsigned char* smem, int heapOff, int maxBatches) {
+__device__ bool run_sssp(const H& heap, Inst* in, unsigned char* smem, int heapOff, int maxBatches) {
     const int B = heap.batchSize, T = blockDim.x, tid = threadIdx.x;
     u64* batch = reinterpret_cast<u64*>(smem);
     u64* emit = batch + B;
@@ -551,8 +495,9 @@ __device__ void run_sssp(const H& heap, Inst* in, unsigned char* smem, int heapO
     int lastBusy = -1, batches = 0;
     if (tid == 0) ctl[1] = 0;
     __syncthreads();
+    bool over = true;  // false: the batch budget ran out, the search goes on
     for (;;) {
-        if (maxBatches && batches++ == maxBatches) break;
+        if (maxBatches && batches++ == maxBatches) { over = false; break; }
         if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart)) break;
         int size = 0;
         heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, heapOff);
@@ -568,7 +513,462 @@ __device__ void run_sssp(const H& heap, Inst* in, unsigned char* smem, int heapO
         atomicAdd(&in->expanded, edges);
         atomicAdd(&in->inserted, inserted);
     }
+    return over;
 }
+
+// One block per instance, after a launch or once the last block has left
+// it: records failures from the heap's error word, marks the search done
+// when its heap holds no key below the prune threshold, and for a finished
+// SSSP counts the reachable vertices and sums their distances (the query's
+// digest).  final != 0: the search was run to the end, so a heap with a key
+// below the threshold is an error.  Every thread of the block calls it;
+// loads go to L2, so a block that ran other instances before reads no
+// stale lines.
+__device__ inline void collect_instance(Inst* in, int final, int batchSize) {
+    __shared__ int s_done;
+    __shared__ unsigned long long s_red[2][32];
+    if (threadIdx.x == 0) {
+        gh::HeapState* st = in->state;
+        const int err = __ldcg(&st->err);
+        if (err && !in->failed)
+            in->failed = err == gh::kErrCapacity ? GH_ERR_CAPACITY : err == gh::kErrTimeout ? GH_ERR_TIMEOUT : GH_ERR_STATE;
+        const int bc = __ldcg(&st->batchCount);
+        const bool empty = bc == 0 && __ldcg(&st->partialBufferSize) == 0;
+        const bool ringEmpty = in->fifo == nullptr || __ldcg(&in->fifo->end) == __ldcg(&in->fifo->begin);
+        const bool finished = (empty || __ldcg(&in->items[bc > 0 ? batchSize : 0]) >= prune_threshold(in)) && ringEmpty;
+        if (in->fifo && __ldcg(&in->fifo->err) && !in->failed) in->failed = GH_ERR_TIMEOUT;
+        const int stop = __ldcg(&in->stop);
+        if (final && !in->failed && !finished && !stop) in->failed = GH_ERR_STATE;
+        in->done = in->failed || stop || finished;
+        s_done = in->done && !in->failed && in->kind == GH_SEARCH_SSSP;
+    }
+    __syncthreads();
+    if (s_done) {
+        unsigned long long cnt = 0, sum = 0;
+        for (int v = threadIdx.x; v < in->nv; v += blockDim.x) {
+            const unsigned dv = __ldcg(in->g + v);
+            if (dv != 0xffffffffu) { ++cnt; sum += dv; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+            sum += __shfl_down_sync(0xffffffffu, sum, o);
+        }
+        if ((threadIdx.x & 31) == 0) { s_red[0][threadIdx.x >> 5] = cnt; s_red[1][threadIdx.x >> 5] = sum; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long c = 0, s2 = 0;
+            for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) { c += s_red[0][w]; s2 += s_red[1][w]; }
+            in->reached = c;
+            in->distSum = s2;
+        }
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------ served, device loop
+// Thread 0 of a block runs the control steps below; the state they share
+// lives in ServeDev.  Three kinds of state:
+//  * the admission state (pending requests, free slots, free arena ranges,
+//    counters): only the holder of ServeDev::lock reads or writes it, with
+//    volatile accesses (no stale L1 lines across blocks);
+//  * the work-token queue: a bounded ring of cells, each with a sequence
+//    word (cell i of lap k is free at seq i + k * cap, holds a token at
+//    seq i + k * cap + 1); producers take a position with atomicAdd,
+//    consumers with compare-and-swap, and the sequence words carry the
+//    release/acquire order from the producer to the consumer;
+//  * the rings in pinned host memory: records are filled first and their
+//    sequence word is stored last with system-scope release; the reader
+//    loads the sequence word with system-scope acquire.
+// Every wait has a limit (waitNs for the lock and a queue cell, stallNs for
+// a work token while no token moves); a wait that runs out records an error
+// and makes every block leave.
+namespace sv {
+
+__device__ __forceinline__ u64 ld_acquire_sys(const u64* p) {
+    u64 v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ u64 ld_relaxed_sys(const u64* p) {
+    u64 v;
+    asm volatile("ld.relaxed.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_relaxed_sys(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.sys.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_sys(u64* p, u64 v) {
+    asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_sys(u64* p, u64 v) {
+    asm volatile("st.relaxed.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_sys(int* p, int v) {
+    asm volatile("st.relaxed.sys.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ u64 ld_acquire_gpu(const u64* p) {
+    u64 v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ u64 ld_relaxed_gpu(const u64* p) {
+    u64 v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(u64* p, u64 v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Records a loop error and makes every block leave.
+__device__ inline void fail(ServeDev* d, int code) {
+    atomicCAS(&d->err, 0, code);
+    st_relaxed_sys(&d->host->err, code);
+    atomicExch(&d->exit, 1);
+}
+
+__device__ inline bool leaving(ServeDev* d) { return ld_relaxed_gpu(&d->exit) != 0; }
+
+// Appends a token.  The ring has a cell for every token that can be out
+// at once, so the cell is free or about to be (its last consumer is
+// between its compare-and-swap and its release).
+__device__ inline bool push(ServeDev* d, int v) {
+    const u64 pos = atomicAdd(&d->enq, 1ull);
+    ServeCell* c = d->cells + (pos & d->cellMask);
+    const u64 t0 = gh::detail::globaltimer();
+    while (ld_acquire_gpu(&c->seq) != pos) {
+        if (gh::detail::globaltimer() - t0 > static_cast<u64>(d->waitNs)) {
+            fail(d, kServeErrQueue);
+            return false;
+        }
+        __nanosleep(64);
+    }
+    c->val = v;
+    st_release_gpu(&c->seq, pos + 1);
+    return true;
+}
+
+// Takes the oldest token, or returns -1 if none is ready.  An empty poll
+// uses relaxed loads only; the acquire comes once a token is taken (an
+// acquire load may drop the SM's L1 lines, which the blocks searching
+// beside this one are using).
+__device__ inline int pop(ServeDev* d) {
+    for (int tries = 0; tries < 32; ++tries) {
+        const u64 pos = ld_relaxed_gpu(&d->deq);
+        ServeCell* c = d->cells + (pos & d->cellMask);
+        const u64 s = ld_relaxed_gpu(&c->seq);
+        if (s == pos + 1) {
+            if (atomicCAS(&d->deq, pos, pos + 1) == pos) {
+                ld_acquire_gpu(&c->seq);  // orders what the producer wrote before its release
+                const int v = ld_relaxed_gpu(&c->val);
+                st_release_gpu(&c->seq, pos + d->cellMask + 1);
+                return v;
+            }
+        } else if (s < pos + 1) {
+            return -1;  // empty, or its producer has not stored it yet
+        }
+    }
+    return -1;
+}
+
+__device__ inline bool try_lock(ServeDev* d) {
+    if (atomicCAS(&d->lock, 0, 1) != 0) return false;
+    __threadfence();
+    return true;
+}
+
+__device__ inline bool lock(ServeDev* d) {
+    const u64 t0 = gh::detail::globaltimer();
+    while (atomicCAS(&d->lock, 0, 1) != 0) {
+        if (gh::detail::globaltimer() - t0 > static_cast<u64>(d->waitNs)) {
+            fail(d, kServeErrLock);
+            return false;
+        }
+        __nanosleep(128);
+    }
+    __threadfence();
+    return true;
+}
+
+__device__ inline void unlock(ServeDev* d) {
+    __threadfence();
+    atomicExch(&d->lock, 0);
+}
+
+// 96-byte request records, word by word.
+__device__ inline void copy_req(volatile ServeReq* dst, const volatile ServeReq* src) {
+    volatile u64* o = reinterpret_cast<volatile u64*>(dst);
+    const volatile u64* i = reinterpret_cast<const volatile u64*>(src);
+    for (int k = 0; k < static_cast<int>(sizeof(ServeReq) / 8); ++k) o[k] = i[k];
+}
+
+__device__ inline void copy_req_from_host(volatile ServeReq* dst, const ServeReq* src) {
+    volatile u64* o = reinterpret_cast<volatile u64*>(dst);
+    const u64* i = reinterpret_cast<const u64*>(src);
+    for (int k = 0; k < static_cast<int>(sizeof(ServeReq) / 8); ++k) o[k] = ld_relaxed_sys(i + k);
+}
+
+// First fit over the free ranges, kept sorted by offset (lock held).
+__device__ inline bool arena_alloc(ServeDev* d, u64 bytes, u64* off) {
+    volatile ServeRange* r = d->ranges;
+    volatile ServeDev* v = d;
+    const int n = v->nranges;
+    for (int k = 0; k < n; ++k) {
+        if (r[k].len < bytes) continue;
+        *off = r[k].off;
+        r[k].off = r[k].off + bytes;
+        r[k].len = r[k].len - bytes;
+        if (r[k].len == 0) {
+            for (int j = k; j + 1 < n; ++j) { r[j].off = r[j + 1].off; r[j].len = r[j + 1].len; }
+            v->nranges = n - 1;
+        }
+        return true;
+    }
+    return false;
+}
+
+// Returns a block, merging it with its neighbours (lock held).  There are
+// at most one more free ranges than allocated blocks, so the array of
+// maxSlots + 2 never overflows.
+__device__ inline void arena_free(ServeDev* d, u64 off, u64 bytes) {
+    volatile ServeRange* r = d->ranges;
+    volatile ServeDev* v = d;
+    const int n = v->nranges;
+    int k = 0;
+    while (k < n && r[k].off < off) ++k;
+    const bool prev = k > 0 && r[k - 1].off + r[k - 1].len == off;
+    const bool next = k < n && off + bytes == r[k].off;
+    if (prev && next) {
+        r[k - 1].len = r[k - 1].len + bytes + r[k].len;
+        for (int j = k; j + 1 < n; ++j) { r[j].off = r[j + 1].off; r[j].len = r[j + 1].len; }
+        v->nranges = n - 1;
+    } else if (prev) {
+        r[k - 1].len = r[k - 1].len + bytes;
+    } else if (next) {
+        r[k].off = off;
+        r[k].len = r[k].len + bytes;
+    } else if (n < d->maxRanges) {
+        for (int j = n; j > k; --j) { r[j].off = r[j - 1].off; r[j].len = r[j - 1].len; }
+        r[k].off = off;
+        r[k].len = bytes;
+        v->nranges = n + 1;
+    }
+}
+
+// The host's view of the admission state (lock held).
+__device__ inline void publish_status(ServeDev* d) {
+    volatile ServeDev* v = d;
+    ServeHost* h = d->host;
+    st_relaxed_sys(reinterpret_cast<u64*>(&h->usedBytes), v->usedBytes);
+    st_relaxed_sys(&h->slotsUsed, d->maxSlots - v->nfree);
+    st_relaxed_sys(&h->pending, v->npend);
+    st_relaxed_sys(&h->active, v->active);
+    st_relaxed_sys(&h->admitted, v->admitted);
+}
+
+// Admission (lock held): the host's stop word, new requests out of the
+// ring, then the pending requests in arrival order into free slots and
+// memory (skipping those that do not fit yet), each admitted one as a setup
+// token; last, the idle limit.
+__device__ inline void admit(ServeDev* d) {
+    volatile ServeDev* v = d;
+    ServeHost* h = d->host;
+    if (ld_relaxed_sys(&h->stop) != 0) {
+        atomicExch(&d->exit, 1);
+        return;
+    }
+    const u64 mask = static_cast<u64>(d->ringCap) - 1;
+    u64 taken = v->reqTaken;
+    int np = v->npend;
+    bool changed = false;
+    while (np < d->ringCap) {
+        const ServeReq* r = d->ring + (taken & mask);
+        if (ld_acquire_sys(&r->seq) != taken + 1) break;
+        copy_req_from_host(d->pend + np, r);
+        ++np;
+        ++taken;
+        changed = true;
+    }
+    if (changed) {
+        v->reqTaken = taken;
+        v->npend = np;
+        st_release_sys(&h->reqTaken, taken);  // the records below `taken` may be written again
+    }
+    if (changed || v->freeEpoch != v->admitEpoch) {
+        v->admitEpoch = v->freeEpoch;
+        volatile int* freeSlots = d->freeSlots;
+        int j = 0;
+        for (int i = 0; i < np; ++i) {
+            volatile ServeReq* q = d->pend + i;
+            u64 off = 0;
+            if (v->nfree > 0 && arena_alloc(d, q->bytes, &off)) {
+                const int nf = v->nfree - 1;
+                const int slot = freeSlots[nf];
+                v->nfree = nf;
+                q->off = off;
+                copy_req(d->slotReq + slot, q);
+                v->active = v->active + 1;
+                v->usedBytes = v->usedBytes + q->bytes;
+                v->admitted = v->admitted + 1;
+                changed = true;
+                if (!push(d, slot | kServeSetup)) return;
+                continue;
+            }
+            if (j != i) copy_req(d->pend + j, q);
+            ++j;
+        }
+        v->npend = j;
+    }
+    if (changed) publish_status(d);
+    const u64 now = gh::detail::globaltimer();
+    if (v->npend == 0 && v->active == 0) {
+        if (v->idleSince == 0) v->idleSince = now;
+        else if (now - v->idleSince > static_cast<u64>(d->idleNs)) atomicExch(&d->exit, 1);
+    } else {
+        v->idleSince = 0;
+    }
+    if (!changed) atomicExch(&d->admitAt, now + 1000);  // nothing new: let the others run for a microsecond
+}
+
+// Thread 0: the next token for this block, or -1 when the blocks leave.
+__device__ inline int next_token(ServeDev* d) {
+    u64 lastDeq = ~0ull, since = 0;
+    unsigned backoff = 32;
+    for (;;) {
+        if (leaving(d)) return -1;
+        const u64 now = gh::detail::globaltimer();
+        if (now >= ld_relaxed_gpu(&d->admitAt) && try_lock(d)) {
+            admit(d);
+            unlock(d);
+            if (leaving(d)) return -1;
+        }
+        const int t = pop(d);
+        if (t >= 0) return t;
+        const u64 dq = ld_relaxed_gpu(&d->deq);
+        if (dq != lastDeq) {
+            lastDeq = dq;
+            since = now;
+        } else if (now - since > static_cast<u64>(d->stallNs)) {
+            fail(d, kServeErrWait);
+            return -1;
+        }
+        __nanosleep(backoff);
+        backoff = backoff < 2048 ? backoff * 2 : 2048;
+    }
+}
+
+// Block-wide: the instance record of an admitted query from its request
+// and its arena block, the reset of its arrays, its seed, then its search
+// tokens.
+__device__ inline void setup_query(ServeDev* d, int slot, int B) {
+    Inst* in = d->insts + slot;
+    __shared__ int s_blocks;
+    if (threadIdx.x == 0) {
+        const volatile ServeReq* q = d->slotReq + slot;
+        const int kind = q->kind, bn = q->bn;
+        const long long dist = kind == GH_SEARCH_SSSP ? static_cast<long long>(q->n)
+                                                      : static_cast<long long>(q->width) * q->height;
+        const QueryLayout L = query_layout(bn, B, dist);
+        unsigned char* base = d->arena + q->off;
+        u64* words = reinterpret_cast<u64*>(in);
+        for (int k = 0; k < static_cast<int>(sizeof(Inst) / 8); ++k) words[k] = 0;
+        in->kind = kind;
+        in->blocks = q->blocks;
+        in->batchNum = bn;
+        in->state = reinterpret_cast<gh::HeapState*>(base);
+        in->items = reinterpret_cast<u64*>(base + L.items);
+        in->status = reinterpret_cast<int*>(base + L.status);
+        in->g = reinterpret_cast<unsigned*>(base + L.g);
+        if (kind == GH_SEARCH_SSSP) {
+            in->nv = q->n;
+            in->source = q->a;
+            in->rowptr = q->rowptr;
+            in->col = q->col;
+            in->wt = q->w;
+        } else {
+            in->width = q->width;
+            in->height = q->height;
+            in->cost = q->cost;
+            in->start = q->a;
+            in->goal = q->b;
+        }
+        in->tokens = q->blocks;
+        s_blocks = q->blocks;
+    }
+    __syncthreads();
+    fill_instance(in, B, threadIdx.x, blockDim.x);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        seed_instance(in);
+        __threadfence();
+        for (int k = 0; k < s_blocks; ++k)
+            if (!push(d, slot)) break;
+    }
+    __syncthreads();
+}
+
+// Thread 0, after the last token of a query came back: the result, the
+// slot and memory back to the free lists, then the completion record.
+__device__ inline void complete(ServeDev* d, Inst* in, int slot) {
+    volatile ServeDev* v = d;
+    const volatile ServeReq* q = d->slotReq + slot;
+    const long long qid = q->qid;
+    const u64 off = q->off, bytes = q->bytes;
+    const int failed = in->failed;
+    const u64 r0 = in->kind == GH_SEARCH_SSSP ? in->reached : static_cast<u64>(static_cast<unsigned>(__ldcg(&in->incumbent)));
+    const u64 r1 = in->kind == GH_SEARCH_SSSP ? in->distSum : 0;
+    if (!lock(d)) return;
+    arena_free(d, off, bytes);
+    volatile int* freeSlots = d->freeSlots;
+    freeSlots[v->nfree] = slot;
+    v->nfree = v->nfree + 1;
+    v->active = v->active - 1;
+    v->usedBytes = v->usedBytes - bytes;
+    v->freeEpoch = v->freeEpoch + 1;
+    const u64 c = v->doneClaim;
+    v->doneClaim = c + 1;
+    publish_status(d);
+    st_relaxed_sys(&d->host->completed, c + 1);
+    unlock(d);
+    atomicExch(&d->admitAt, 0ull);  // memory came free: admit at once
+    ServeDone* r = d->done + (c & (static_cast<u64>(d->ringCap) - 1));
+    st_relaxed_sys(reinterpret_cast<u64*>(&r->qid), static_cast<u64>(qid));
+    st_relaxed_sys(&r->state, failed ? 3 : 2);
+    st_relaxed_sys(&r->failed, failed);
+    st_relaxed_sys(&r->r0, r0);
+    st_relaxed_sys(&r->r1, r1);
+    st_relaxed_sys(&r->tDone, gh::detail::globaltimer());
+    st_release_sys(&r->seq, c + 1);
+}
+
+// Block-wide, after a stint on a query: its token goes back into the queue
+// while the search goes on; once it is over, the block that returns the
+// last token collects the result and completes the query.
+__device__ inline void end_stint(ServeDev* d, Inst* in, int slot, bool over, int B) {
+    __shared__ int s_last;
+    if (threadIdx.x == 0) {
+        __threadfence();  // this block's writes to the query before its token moves on
+        s_last = 0;
+        if (!over) push(d, slot);
+        else s_last = atomicSub(&in->tokens, 1) == 1;
+        if (s_last) __threadfence();
+    }
+    __syncthreads();
+    if (s_last) {
+        collect_instance(in, 1, B);
+        if (threadIdx.x == 0) complete(d, in, slot);
+    }
+    __syncthreads();
+}
+
+}  // namespace sv
 
 // Resident blocks per SM the build of the search kernel for blocks of up to
 // 256 threads is compiled for (512-thread blocks: one).  On the batched
@@ -577,148 +977,59 @@ __device__ void run_sssp(const H& heap, Inst* in, unsigned char* smem, int heapO
 // 1774 ms: resident blocks matter more than spills.
 constexpr int kSmallSearchBlocksPerSM = 3;
 
-// maxBatches > 0: each task takes at most that many batches, then the block
-// moves on (the search resumes in a later launch from its heap).  MaxT is
-// the largest block it runs with; the register budget follows from it and
-// the blocks each SM should hold.
+// The persistent search launch.  Without args.serve, blocks take instances
+// from a task list (an instance appears once per block it should get);
+// with it, they take work tokens from the device loop's queue (setup
+// tokens, and one search token per block a query should get), until the
+// loop's exit word is set.  args.maxBatches > 0: a block takes at most that
+// many batches of a query, then moves on (the search resumes later from its
+// heap).  MaxT is the largest block it runs with; the register budget
+// follows from it and the blocks each SM should hold.
 template <typename H, int MaxT>
-__global__ void __launch_bounds__(MaxT, MaxT <= 256 ? kSmallSearchBlocksPerSM : 1)
-    k_search(H proto, Inst* insts, const int* tasks, int ntasks, int* next, int maxBatches) {
+__global__ void __launch_bounds__(MaxT, MaxT <= 256 ? kSmallSearchBlocksPerSM : 1) k_search(H proto, SearchArgs args) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_task;
     const int heapOff = static_cast<int>(SearchSmem::bytes(proto.batchSize, blockDim.x) / 4);
     for (;;) {
-        if (threadIdx.x == 0) s_task = atomicAdd(next, 1);
+        if (threadIdx.x == 0) {
+            if (args.serve) {
+                s_task = sv::next_token(args.serve);
+            } else {
+                const int t = atomicAdd(args.next, 1);
+                s_task = t < args.ntasks ? args.tasks[t] : -1;
+            }
+        }
         __syncthreads();
-        const int t = s_task;
+        const int task = s_task;
         __syncthreads();
-        if (t >= ntasks) break;
-        Inst* in = insts + tasks[t];
+        if (task < 0) break;
+        if (task & kServeSetup) {
+            sv::setup_query(args.serve, task & ~kServeSetup, proto.batchSize);
+            continue;
+        }
+        Inst* in = args.insts + task;
         H h = proto;
         h.heapItems = reinterpret_cast<typename H::key_type*>(in->items);
         h.status = in->status;
         h.state = in->state;
         h.batchNum = in->batchNum;
-        if (in->kind == GH_SEARCH_ASTAR) run_astar(h, in, smem, heapOff, maxBatches);
-        else if (in->kind == GH_SEARCH_SSSP) run_sssp(h, in, smem, heapOff, maxBatches);
-        else run_knapsack(h, in, smem, heapOff, maxBatches);
+        bool over;
+        if (in->kind == GH_SEARCH_ASTAR) over = run_astar(h, in, smem, heapOff, args.maxBatches);
+        else if (in->kind == GH_SEARCH_SSSP) over = run_sssp(h, in, smem, heapOff, args.maxBatches);
+        else over = run_knapsack(h, in, smem, heapOff, args.maxBatches);
         __syncthreads();
+        if (args.serve) sv::end_stint(args.serve, in, task, over, proto.batchSize);
     }
 }
 
-// After a launch, one block per listed instance (ids == NULL: instance
-// blockIdx.x): records failures from the heap's error word, marks the
-// search done when its heap holds no key below the prune threshold (no
-// block is inside it once the launch has ended), and for a finished SSSP
-// counts the reachable vertices and sums their distances (the query's
-// digest).  final != 0: every search was run to the end, so a heap with a
-// key below the threshold is an error.
-__global__ void k_search_collect(Inst* insts, const int* ids, int final, int batchSize) {
-    Inst* in = insts + (ids ? ids[blockIdx.x] : static_cast<int>(blockIdx.x));
-    __shared__ int s_done;
-    __shared__ unsigned long long s_red[2][32];
-    if (threadIdx.x == 0) {
-        const int err = in->state->err;
-        if (err && !in->failed)
-            in->failed = err == gh::kErrCapacity ? GH_ERR_CAPACITY : err == gh::kErrTimeout ? GH_ERR_TIMEOUT : GH_ERR_STATE;
-        const int bc = in->state->batchCount;
-        const bool empty = bc == 0 && in->state->partialBufferSize == 0;
-        const bool ringEmpty = in->fifo == nullptr || in->fifo->end == in->fifo->begin;
-        const bool finished = (empty || in->items[bc > 0 ? batchSize : 0] >= prune_threshold(in)) && ringEmpty;
-        if (in->fifo && in->fifo->err && !in->failed) in->failed = GH_ERR_TIMEOUT;
-        if (final && !in->failed && !finished && !in->stop) in->failed = GH_ERR_STATE;
-        in->done = in->failed || in->stop || finished;
-        s_done = in->done && !in->failed && in->kind == GH_SEARCH_SSSP;
-    }
-    __syncthreads();
-    if (!s_done) return;
-    unsigned long long cnt = 0, sum = 0;
-    for (int v = threadIdx.x; v < in->nv; v += blockDim.x) {
-        const unsigned dv = in->g[v];
-        if (dv != 0xffffffffu) { ++cnt; sum += dv; }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-        sum += __shfl_down_sync(0xffffffffu, sum, o);
-    }
-    if ((threadIdx.x & 31) == 0) { s_red[0][threadIdx.x >> 5] = cnt; s_red[1][threadIdx.x >> 5] = sum; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long c = 0, s2 = 0;
-        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) { c += s_red[0][w]; s2 += s_red[1][w]; }
-        in->reached = c;
-        in->distSum = s2;
-    }
-}
-
-// The search kernel built for `threads` threads per block.
-template <typename H>
-inline auto search_kernel(int threads) {
-    return threads <= 256 ? k_search<H, 256> : k_search<H, kMaxSearchThreads>;
-}
-
-template <typename H>
-cudaError_t launch_search(const H& proto, Inst* insts, const int* tasks, int ntasks, int* next, int grid, int threads,
-                          size_t smem, cudaStream_t s, int maxBatches) {
-    const auto kern = search_kernel<H>(threads);
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    kern<<<grid, threads, smem, s>>>(proto, insts, tasks, ntasks, next, maxBatches);
-    gh::impl::count_launch();
-    return cudaGetLastError();
-}
-
-// Host side: shape of a search launch, shared by the batched and served forms.
-struct SearchConfig {
-    int batchSize;
-    int variant;
-    int threads;  // 0 = min(batchSize, kMaxSearchThreads)
-    long long timeoutNs;
-    int numSMs;
-};
-
-inline int search_threads(const SearchConfig& c) {
-    return c.threads ? c.threads : (c.batchSize < kMaxSearchThreads ? c.batchSize : kMaxSearchThreads);
-}
-
-inline size_t search_smem(const SearchConfig& c) {
-    return SearchSmem::bytes(c.batchSize, search_threads(c)) + 16 + gh::Heap<uint64_t, 0, true>::smemBytes(c.batchSize);
-}
-
-// Calls f(Heap<uint64_t, variant, true, IPT>{}) for the configuration's layout and merge width.
-template <typename F>
-inline cudaError_t search_dispatch(const SearchConfig& c, F&& f) {
-    const int ipt = 2 * c.batchSize / search_threads(c);
-    if (c.variant == GH_TOPDOWN) {
-        if (ipt == 2) return f(gh::Heap<uint64_t, gh::kTopDown, true, 2>{});
-        if (ipt == 4) return f(gh::Heap<uint64_t, gh::kTopDown, true, 4>{});
-    } else {
-        if (ipt == 2) return f(gh::Heap<uint64_t, gh::kBottomUp, true, 2>{});
-        if (ipt == 4) return f(gh::Heap<uint64_t, gh::kBottomUp, true, 4>{});
-    }
-    return cudaErrorInvalidValue;
-}
-
-// Blocks of one persistent launch: resident blocks per SM x SMs.
-inline int search_resident_blocks(const SearchConfig& c) {
-    int per = 0;
+// Launch of the search kernel for one heap layout, the merge width following
+// from the batch size and block threads.
+template <int Variant>
+inline cudaError_t launch_layout(const SearchConfig& c, const SearchArgs& a, int grid, cudaStream_t s) {
     const int T = search_threads(c);
     const size_t smem = search_smem(c);
-    cudaError_t e = search_dispatch(c, [&](auto proto) {
-        using H = decltype(proto);
-        const auto kern = search_kernel<H>(T);
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, T, smem);
-    });
-    if (e != cudaSuccess || per < 1) per = 1;
-    return per * c.numSMs;
-}
-
-inline cudaError_t search_launch(const SearchConfig& c, Inst* insts, const int* tasks, int ntasks, int* next, int grid,
-                                 cudaStream_t s, int maxBatches) {
-    const int T = search_threads(c);
-    const size_t smem = search_smem(c);
-    return search_dispatch(c, [&](auto h) {
+    auto go = [&](auto h) -> cudaError_t {
+        using H = decltype(h);
         h.heapItems = nullptr;
         h.status = nullptr;
         h.state = nullptr;
@@ -727,9 +1038,36 @@ inline cudaError_t search_launch(const SearchConfig& c, Inst* insts, const int* 
         h.batchSize = c.batchSize;
         h.sortOutput = 0;
         h.timeoutNs = c.timeoutNs;
-        return launch_search(h, insts, tasks, ntasks, next, grid, T, smem, s, maxBatches);
-    });
+        const auto kern = T <= 256 ? k_search<H, 256> : k_search<H, kMaxSearchThreads>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        kern<<<grid, T, smem, s>>>(h, a);
+        gh::impl::count_launch();
+        return cudaGetLastError();
+    };
+    const int ipt = 2 * c.batchSize / T;
+    if (ipt == 2) return go(gh::Heap<uint64_t, Variant, true, 2>{});
+    if (ipt == 4) return go(gh::Heap<uint64_t, Variant, true, 4>{});
+    return cudaErrorInvalidValue;
 }
 
-}  // namespace
+template <int Variant>
+inline int blocks_per_sm_layout(const SearchConfig& c) {
+    const int T = search_threads(c);
+    const size_t smem = search_smem(c);
+    auto occ = [&](auto h) -> int {
+        using H = decltype(h);
+        const auto kern = T <= 256 ? k_search<H, 256> : k_search<H, kMaxSearchThreads>;
+        int per = 0;
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, T, smem) != cudaSuccess) return 1;
+        return per;
+    };
+    const int ipt = 2 * c.batchSize / T;
+    if (ipt == 2) return occ(gh::Heap<uint64_t, Variant, true, 2>{});
+    if (ipt == 4) return occ(gh::Heap<uint64_t, Variant, true, 4>{});
+    return 1;
+}
 
+}  // namespace search
+}  // namespace gh

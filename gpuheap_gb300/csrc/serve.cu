@@ -13,6 +13,15 @@
 // search_kernels.cuh (the reference's per-query kernels:
 // applications/sssp_longfei_new/sssp.cu:19-132, artifacts/astar/
 // pq_model.cuh:299-371).
+//
+// The device loop (gh_serve_start / gh_serve_poll / gh_serve_stop) moves
+// admission, the steps and collection onto the device: the host writes
+// requests into a ring in pinned host memory and reads completions from
+// another; one resident launch of the search kernel admits, sets up, runs,
+// collects and frees queries (search_kernels.cuh, namespace sv) and leaves
+// after an idle limit or on the host's stop word.  It replaces the host
+// relaunch loop of the reference's A* driver (artifacts/astar/
+// astar_main.cu:127-179), which launches and synchronizes once per round.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,14 +34,18 @@
 #include <vector>
 
 #include "gpuheap.h"
-#include "search_kernels.cuh"
+#include "heap_kernels.cuh"
+#include "search_common.cuh"
 #include "trace.cuh"
+
+using namespace gh::search;
 
 namespace {
 
 struct Dataset {
     int kind;  // GH_SEARCH_SSSP graph or GH_SEARCH_ASTAR map
     int n = 0, width = 0, height = 0;
+    long long m = 0;  // edges of a graph
     const long long* rowptr = nullptr;
     const int* col = nullptr;
     const unsigned* w = nullptr;
@@ -83,6 +96,20 @@ struct gh_server {
     long long steps = 0;
     int* hostTasks = nullptr;  // pinned
     int* hostIds = nullptr;    // pinned
+    // device loop
+    bool resident = false, running = false, paused = false;
+    cudaStream_t loopStream = nullptr;
+    cudaEvent_t loopDone = nullptr;
+    long long idleNs = 100000000LL;
+    int ringCap = 4096, tokensPerQuery = 1;
+    unsigned char* pinned = nullptr;  // request ring, completion ring, host words (mapped)
+    ServeReq* ring = nullptr;
+    ServeDone* done = nullptr;
+    ServeHost* hostw = nullptr;
+    unsigned char* loopMem = nullptr;  // ServeDev and its arrays (device)
+    ServeDev* dev = nullptr;
+    unsigned long long posted = 0, consumed = 0;
+    long long launches = 0;
 };
 
 namespace {
@@ -125,7 +152,9 @@ void size_query(const gh_server* s, Query& q) {
     const Dataset& d = s->data[q.dataset];
     long long keys, dist;
     if (q.kind == GH_SEARCH_SSSP) {
-        keys = std::max<long long>(4LL * d.n, 16LL * B);
+        // the standalone SSSP's bound: label correction can hold several
+        // keys per vertex (half the edges on R-MAT graphs)
+        keys = std::max({4LL * d.n, d.m / 2, 16LL * B});
         dist = d.n;
         q.blocks = static_cast<int>(std::min<long long>(s->ssspMaxBlocks, std::max<long long>(1, d.n / s->ssspPerBlock)));
     } else {
@@ -135,11 +164,7 @@ void size_query(const gh_server* s, Query& q) {
         q.blocks = static_cast<int>(std::min<long long>(s->astarMaxBlocks, std::max<long long>(1, dist / s->astarPerBlock)));
     }
     q.bn = pow2_nodes(keys, B);
-    size_t b = align_up(sizeof(gh::HeapState), 256);
-    b += align_up(static_cast<size_t>(q.bn + 1) * B * 8, 256);
-    b += align_up(static_cast<size_t>(q.bn + 2) * 4, 256);
-    b += align_up(static_cast<size_t>(dist) * 4, 256);
-    q.bytes = b;
+    q.bytes = query_layout(q.bn, B, dist).bytes;
 }
 
 // Instance record of an admitted query at arena offset q.off.
@@ -147,18 +172,16 @@ Inst make_inst(gh_server* s, const Query& q) {
     const int B = s->cfg.batchSize;
     const Dataset& d = s->data[q.dataset];
     unsigned char* p = s->arena + q.off;
+    const QueryLayout L = query_layout(q.bn, B, q.kind == GH_SEARCH_SSSP ? d.n : static_cast<long long>(d.width) * d.height);
     Inst in;
     std::memset(&in, 0, sizeof(in));
     in.kind = q.kind;
     in.blocks = q.blocks;
     in.batchNum = q.bn;
     in.state = reinterpret_cast<gh::HeapState*>(p);
-    p += align_up(sizeof(gh::HeapState), 256);
-    in.items = reinterpret_cast<u64*>(p);
-    p += align_up(static_cast<size_t>(q.bn + 1) * B * 8, 256);
-    in.status = reinterpret_cast<int*>(p);
-    p += align_up(static_cast<size_t>(q.bn + 2) * 4, 256);
-    in.g = reinterpret_cast<unsigned*>(p);
+    in.items = reinterpret_cast<u64*>(p + L.items);
+    in.status = reinterpret_cast<int*>(p + L.status);
+    in.g = reinterpret_cast<unsigned*>(p + L.g);
     if (q.kind == GH_SEARCH_SSSP) {
         in.nv = d.n;
         in.source = q.a;
@@ -179,6 +202,144 @@ Inst make_inst(gh_server* s, const Query& q) {
     do {                                               \
         if ((call) != cudaSuccess) return GH_ERR_CUDA; \
     } while (0)
+
+// ------------------------------------------------------------ device loop
+
+// Writes waiting queries into the request ring while it has room: a record
+// may be written again once its completion has been read, so at most
+// ringCap queries are between posting and reading their completion (the
+// device's pending array and the completion ring have ringCap entries).
+void post_requests(gh_server* s) {
+    const int B = s->cfg.batchSize;
+    while (!s->waiting.empty() && s->posted - s->consumed < static_cast<unsigned long long>(s->ringCap)) {
+        const long long id = s->waiting.front();
+        s->waiting.pop_front();
+        Query& q = s->queries[id];
+        const Dataset& d = s->data[q.dataset];
+        ServeReq* r = s->ring + (s->posted & static_cast<unsigned long long>(s->ringCap - 1));
+        r->qid = id;
+        r->kind = q.kind;
+        r->a = q.a;
+        r->b = q.b;
+        r->blocks = q.blocks;
+        r->bn = q.bn;
+        r->n = d.n;
+        r->width = d.width;
+        r->height = d.height;
+        r->bytes = query_layout(q.bn, B, q.kind == GH_SEARCH_SSSP ? d.n : static_cast<long long>(d.width) * d.height).bytes;
+        r->off = 0;
+        r->rowptr = d.rowptr;
+        r->col = d.col;
+        r->w = d.w;
+        r->cost = d.cost;
+        __atomic_store_n(&r->seq, s->posted + 1, __ATOMIC_RELEASE);
+        ++s->posted;
+        q.state = 1;
+    }
+}
+
+gh_status launch_loop(gh_server* s) {
+    GH_SCUDA(cudaMemsetAsync(&s->dev->exit, 0, sizeof(int), s->loopStream));
+    GH_SCUDA(cudaMemsetAsync(&s->dev->idleSince, 0, sizeof(unsigned long long), s->loopStream));
+    GH_SCUDA(cudaMemsetAsync(&s->dev->admitAt, 0, sizeof(unsigned long long), s->loopStream));
+    GH_SCUDA(search_launch(s->cfg, SearchArgs{s->insts, nullptr, 0, nullptr, s->batchesPerStep, s->dev}, s->grid,
+                           s->loopStream));
+    GH_SCUDA(cudaEventRecord(s->loopDone, s->loopStream));
+    s->running = true;
+    ++s->launches;
+    return GH_OK;
+}
+
+// The stop word makes the admitting block set the exit word; blocks leave
+// after their current stint, with every unfinished query's tokens back in
+// the queue, so a later launch resumes them.
+gh_status stop_loop(gh_server* s) {
+    __atomic_store_n(&s->hostw->stop, 1, __ATOMIC_RELEASE);
+    const cudaError_t e = cudaEventSynchronize(s->loopDone);
+    __atomic_store_n(&s->hostw->stop, 0, __ATOMIC_RELEASE);
+    s->running = false;
+    return e == cudaSuccess ? GH_OK : GH_ERR_CUDA;
+}
+
+gh_status loop_error(const gh_server* s) {
+    const int err = __atomic_load_n(&s->hostw->err, __ATOMIC_ACQUIRE);
+    return err == kServeOk ? GH_OK : err == kServeErrWait || err == kServeErrLock ? GH_ERR_TIMEOUT : GH_ERR_STATE;
+}
+
+// One-time setup of the device loop: the pinned rings and host words, the
+// loop's device state (free slots, one free range over the whole arena,
+// the token queue's cells at their first lap), its stream and event.
+gh_status init_loop(gh_server* s) {
+    const size_t ringBytes = sizeof(ServeReq) * s->ringCap, doneBytes = sizeof(ServeDone) * s->ringCap;
+    if (cudaHostAlloc(&s->pinned, ringBytes + doneBytes + sizeof(ServeHost), cudaHostAllocMapped) != cudaSuccess) {
+        cudaGetLastError();
+        s->pinned = nullptr;
+        return GH_ERR_CUDA;
+    }
+    std::memset(s->pinned, 0, ringBytes + doneBytes + sizeof(ServeHost));
+    s->ring = reinterpret_cast<ServeReq*>(s->pinned);
+    s->done = reinterpret_cast<ServeDone*>(s->pinned + ringBytes);
+    s->hostw = reinterpret_cast<ServeHost*>(s->pinned + ringBytes + doneBytes);
+    void* dp = nullptr;
+    GH_SCUDA(cudaHostGetDevicePointer(&dp, s->pinned, 0));
+    unsigned char* devPinned = static_cast<unsigned char*>(dp);
+
+    s->tokensPerQuery = std::min(1024, s->grid);
+    unsigned long long cells = 1;
+    while (cells < static_cast<unsigned long long>(s->maxSlots) * s->tokensPerQuery + 1) cells <<= 1;
+    const int maxRanges = s->maxSlots + 2;
+    const size_t devBytes = align_up(sizeof(ServeDev), 256), pendBytes = align_up(sizeof(ServeReq) * s->ringCap, 256),
+                 slotBytes = align_up(sizeof(ServeReq) * s->maxSlots, 256),
+                 freeBytes = align_up(sizeof(int) * s->maxSlots, 256),
+                 rangeBytes = align_up(sizeof(ServeRange) * maxRanges, 256), cellBytes = sizeof(ServeCell) * cells;
+    const size_t total = devBytes + pendBytes + slotBytes + freeBytes + rangeBytes + cellBytes;
+    if (cudaMalloc(&s->loopMem, total) != cudaSuccess) {
+        cudaGetLastError();
+        s->loopMem = nullptr;
+        return GH_ERR_CUDA;
+    }
+    std::vector<unsigned char> img(total, 0);
+    ServeDev* d = reinterpret_cast<ServeDev*>(img.data());
+    unsigned char* base = s->loopMem;
+    size_t at = devBytes;
+    d->pend = reinterpret_cast<ServeReq*>(base + at);
+    at += pendBytes;
+    d->slotReq = reinterpret_cast<ServeReq*>(base + at);
+    at += slotBytes;
+    d->freeSlots = reinterpret_cast<int*>(base + at);
+    int* hostFree = reinterpret_cast<int*>(img.data() + at);
+    for (int i = 0; i < s->maxSlots; ++i) hostFree[i] = s->maxSlots - 1 - i;  // slot 0 is taken first
+    at += freeBytes;
+    d->ranges = reinterpret_cast<ServeRange*>(base + at);
+    ServeRange* hostRanges = reinterpret_cast<ServeRange*>(img.data() + at);
+    hostRanges[0].off = 0;
+    hostRanges[0].len = s->arenaBytes;
+    at += rangeBytes;
+    d->cells = reinterpret_cast<ServeCell*>(base + at);
+    ServeCell* hostCells = reinterpret_cast<ServeCell*>(img.data() + at);
+    for (unsigned long long i = 0; i < cells; ++i) hostCells[i].seq = i;
+    d->ring = reinterpret_cast<ServeReq*>(devPinned);
+    d->done = reinterpret_cast<ServeDone*>(devPinned + ringBytes);
+    d->host = reinterpret_cast<ServeHost*>(devPinned + ringBytes + doneBytes);
+    d->insts = s->insts;
+    d->arena = s->arena;
+    d->arenaBytes = s->arenaBytes;
+    d->cellMask = cells - 1;
+    d->ringCap = s->ringCap;
+    d->maxSlots = s->maxSlots;
+    d->maxRanges = maxRanges;
+    d->batchSize = s->cfg.batchSize;
+    d->nfree = s->maxSlots;
+    d->nranges = 1;
+    d->idleNs = s->idleNs;
+    d->waitNs = 2000000000LL;
+    d->stallNs = 60000000000LL;
+    GH_SCUDA(cudaMemcpy(s->loopMem, img.data(), total, cudaMemcpyHostToDevice));
+    s->dev = reinterpret_cast<ServeDev*>(s->loopMem);
+    GH_SCUDA(cudaStreamCreateWithFlags(&s->loopStream, cudaStreamNonBlocking));
+    GH_SCUDA(cudaEventCreateWithFlags(&s->loopDone, cudaEventDisableTiming));
+    return GH_OK;
+}
 
 }  // namespace
 
@@ -241,6 +402,11 @@ gh_status gh_serve_create(gh_server** out, long long arena_bytes, int max_slots,
 
 gh_status gh_serve_destroy(gh_server* s) {
     if (!s) return GH_ERR_INVALID;
+    if (s->running) stop_loop(s);
+    if (s->loopDone) cudaEventDestroy(s->loopDone);
+    if (s->loopStream) cudaStreamDestroy(s->loopStream);
+    if (s->loopMem) cudaFree(s->loopMem);
+    if (s->pinned) cudaFreeHost(s->pinned);
     if (s->arena) cudaFree(s->arena);
     if (s->ctlMem) cudaFree(s->ctlMem);
     if (s->hostTasks) cudaFreeHost(s->hostTasks);
@@ -267,6 +433,8 @@ gh_status gh_serve_add_graph(gh_server* s, int n, const long long* rowptr_dev, c
     Dataset d;
     d.kind = GH_SEARCH_SSSP;
     d.n = n;
+    if (cudaMemcpy(&d.m, rowptr_dev + n, sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess) return GH_ERR_CUDA;
+    if (d.m < 0) return GH_ERR_INVALID;
     d.rowptr = rowptr_dev;
     d.col = col_dev;
     d.w = w_dev;
@@ -302,16 +470,18 @@ gh_status gh_serve_submit(gh_server* s, int kind, int dataset, int a, int b, lon
     q.b = b;
     size_query(s, q);
     if (q.bytes > s->arenaBytes) return GH_ERR_CAPACITY;
+    if (s->resident) q.blocks = std::min(q.blocks, s->tokensPerQuery);
     const long long id = static_cast<long long>(s->queries.size());
     s->queries.push_back(q);
     s->waiting.push_back(id);
     if (query) *query = id;
+    if (s->resident) post_requests(s);
     return GH_OK;
 }
 
 gh_status gh_serve_step(gh_server* s, void* stream, int* finished, int* active, int* queued) {
     gh::trace::Range range_("gh_serve_step");
-    if (!s) return GH_ERR_INVALID;
+    if (!s || s->resident) return GH_ERR_INVALID;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     s->finished.clear();
     // admission, in arrival order, skipping queries that do not fit yet
@@ -336,12 +506,8 @@ gh_status gh_serve_step(gh_server* s, void* stream, int* finished, int* active, 
     if (!fresh.empty()) {
         for (size_t i = 0; i < fresh.size(); ++i) s->hostIds[i] = fresh[i];
         GH_SCUDA(cudaMemcpyAsync(s->ids, s->hostIds, sizeof(int) * fresh.size(), cudaMemcpyHostToDevice, st));
-        k_search_fill<<<dim3(8, static_cast<unsigned>(fresh.size())), 256, 0, st>>>(s->insts, s->ids, s->cfg.batchSize);
-        gh::impl::count_launch();
-        k_search_seed<<<(static_cast<int>(fresh.size()) + 127) / 128, 128, 0, st>>>(s->insts, s->ids,
-                                                                                     static_cast<int>(fresh.size()));
-        gh::impl::count_launch();
-        GH_SCUDA(cudaGetLastError());
+        GH_SCUDA(search_fill(s->insts, s->ids, static_cast<int>(fresh.size()), s->cfg.batchSize, st));
+        GH_SCUDA(search_seed(s->insts, s->ids, static_cast<int>(fresh.size()), st));
         GH_SCUDA(cudaStreamSynchronize(st));  // hostIds and ids are rewritten below
     }
     // one launch over every admitted query: its blocks, largest first
@@ -359,10 +525,9 @@ gh_status gh_serve_step(gh_server* s, void* stream, int* finished, int* active, 
         GH_SCUDA(cudaMemcpyAsync(s->tasks, s->hostTasks, sizeof(int) * nt, cudaMemcpyHostToDevice, st));
         GH_SCUDA(cudaMemcpyAsync(s->ids, s->hostIds, sizeof(int) * act.size(), cudaMemcpyHostToDevice, st));
         GH_SCUDA(cudaMemsetAsync(s->next, 0, sizeof(int), st));
-        GH_SCUDA(search_launch(s->cfg, s->insts, s->tasks, nt, s->next, std::min(s->grid, nt), st, s->batchesPerStep));
-        k_search_collect<<<static_cast<unsigned>(act.size()), 256, 0, st>>>(s->insts, s->ids, 0, s->cfg.batchSize);
-        gh::impl::count_launch();
-        GH_SCUDA(cudaGetLastError());
+        GH_SCUDA(search_launch(s->cfg, SearchArgs{s->insts, s->tasks, nt, s->next, s->batchesPerStep, nullptr},
+                               std::min(s->grid, nt), st));
+        GH_SCUDA(search_collect(s->insts, s->ids, static_cast<int>(act.size()), 0, s->cfg.batchSize, st));
         GH_SCUDA(cudaMemcpyAsync(s->hinst.data(), s->insts, sizeof(Inst) * s->maxSlots, cudaMemcpyDeviceToHost, st));
         GH_SCUDA(cudaStreamSynchronize(st));
         ++s->steps;
@@ -371,7 +536,10 @@ gh_status gh_serve_step(gh_server* s, void* stream, int* finished, int* active, 
             if (!in.done) continue;
             Query& q = s->queries[s->slotQuery[slot]];
             q.state = in.failed ? 3 : 2;
-            if (q.kind == GH_SEARCH_SSSP) {
+            if (in.failed) {
+                q.r0 = 0;
+                q.r1 = static_cast<unsigned long long>(in.failed);
+            } else if (q.kind == GH_SEARCH_SSSP) {
                 q.r0 = in.reached;
                 q.r1 = in.distSum;
             } else {
@@ -413,6 +581,14 @@ gh_status gh_serve_finished(gh_server* s, long long* ids, int max_ids, int* coun
 
 gh_status gh_serve_info(gh_server* s, long long* used_bytes, long long* free_bytes, int* slots_used, long long* steps) {
     if (!s) return GH_ERR_INVALID;
+    if (s->resident) {
+        const long long used = __atomic_load_n(&s->hostw->usedBytes, __ATOMIC_ACQUIRE);
+        if (used_bytes) *used_bytes = used;
+        if (free_bytes) *free_bytes = static_cast<long long>(s->arenaBytes) - used;
+        if (slots_used) *slots_used = __atomic_load_n(&s->hostw->slotsUsed, __ATOMIC_ACQUIRE);
+        if (steps) *steps = s->launches;
+        return GH_OK;
+    }
     if (used_bytes) *used_bytes = static_cast<long long>(s->used);
     if (free_bytes) *free_bytes = static_cast<long long>(s->arenaBytes - s->used);
     if (slots_used) {
@@ -422,6 +598,78 @@ gh_status gh_serve_info(gh_server* s, long long* used_bytes, long long* free_byt
     }
     if (steps) *steps = s->steps;
     return GH_OK;
+}
+
+
+gh_status gh_serve_start(gh_server* s, int idle_ms) {
+    gh::trace::Range range_("gh_serve_start");
+    if (!s || idle_ms < 1 || idle_ms > 600000) return GH_ERR_INVALID;
+    if (s->resident) {
+        if (s->running) return GH_ERR_INVALID;
+        if (loop_error(s) != GH_OK) return GH_ERR_STATE;
+        s->paused = false;
+        return GH_OK;  // resumes: the next gh_serve_poll launches the loop when there is work
+    }
+    // the device loop takes over the whole arena: no query may be in the host steps
+    for (long long q : s->slotQuery)
+        if (q >= 0) return GH_ERR_INVALID;
+    if (!s->waiting.empty()) return GH_ERR_INVALID;
+    s->idleNs = static_cast<long long>(idle_ms) * 1000000LL;
+    const gh_status st = init_loop(s);
+    if (st != GH_OK) return st;
+    s->resident = true;
+    return GH_OK;
+}
+
+gh_status gh_serve_poll(gh_server* s, int* finished, int* active, int* queued) {
+    gh::trace::Range range_("gh_serve_poll");
+    if (!s || !s->resident) return GH_ERR_INVALID;
+    s->finished.clear();
+    const unsigned long long mask = static_cast<unsigned long long>(s->ringCap - 1);
+    for (;;) {
+        const ServeDone* r = s->done + (s->consumed & mask);
+        if (__atomic_load_n(&r->seq, __ATOMIC_ACQUIRE) != s->consumed + 1) break;
+        const long long id = r->qid;
+        if (id >= 0 && id < static_cast<long long>(s->queries.size())) {
+            Query& q = s->queries[id];
+            q.state = r->state;
+            q.r0 = r->r0;
+            q.r1 = r->state == 3 ? static_cast<unsigned long long>(r->failed) : r->r1;
+            q.finishStep = static_cast<long long>(s->consumed) + 1;  // completion order
+            s->finished.push_back(id);
+        }
+        ++s->consumed;
+    }
+    post_requests(s);
+    if (s->running) {
+        const cudaError_t e = cudaEventQuery(s->loopDone);
+        if (e == cudaSuccess) s->running = false;
+        else if (e != cudaErrorNotReady) return GH_ERR_CUDA;
+    }
+    const gh_status err = loop_error(s);
+    if (err != GH_OK) return err;
+    if (!s->running && !s->paused && s->posted > s->consumed) {
+        const gh_status st = launch_loop(s);
+        if (st != GH_OK) return st;
+    }
+    if (finished) *finished = static_cast<int>(s->finished.size());
+    const int act = __atomic_load_n(&s->hostw->active, __ATOMIC_ACQUIRE);
+    const unsigned long long taken = __atomic_load_n(&s->hostw->reqTaken, __ATOMIC_ACQUIRE);
+    if (active) *active = act;
+    if (queued)
+        *queued = static_cast<int>(s->waiting.size() + (s->posted - taken)) + __atomic_load_n(&s->hostw->pending, __ATOMIC_ACQUIRE);
+    return GH_OK;
+}
+
+gh_status gh_serve_stop(gh_server* s) {
+    gh::trace::Range range_("gh_serve_stop");
+    if (!s || !s->resident) return GH_ERR_INVALID;
+    s->paused = true;
+    if (s->running) {
+        const gh_status st = stop_loop(s);
+        if (st != GH_OK) return st;
+    }
+    return loop_error(s);
 }
 
 }  // extern "C"

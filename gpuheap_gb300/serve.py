@@ -68,6 +68,28 @@ class Server:
         _check(lib().gh_serve_finished(self._h, ids, f.value, ctypes.byref(n)), "serve_finished")
         return [ids[i] for i in range(f.value)], a.value, qd.value
 
+    def start(self, idle_ms=100):
+        """Switches to the device-resident loop: from now on submit() posts
+        into a pinned request ring and poll() collects completions; the
+        loop's launch leaves after idle_ms without work and poll() launches
+        it again when work arrives."""
+        _check(lib().gh_serve_start(self._h, int(idle_ms)), "serve_start")
+
+    def poll(self):
+        """Device loop: completions since the last poll; returns (ids
+        finished, active, queued).  Does not block."""
+        f, a, qd = _I(), _I(), _I()
+        _check(lib().gh_serve_poll(self._h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(qd)), "serve_poll")
+        ids = (_LL * max(1, f.value))()
+        n = _I()
+        _check(lib().gh_serve_finished(self._h, ids, f.value, ctypes.byref(n)), "serve_finished")
+        return [ids[i] for i in range(f.value)], a.value, qd.value
+
+    def stop(self):
+        """Device loop: pauses it (the launch leaves after its blocks'
+        current stints); start() resumes the queries left in it."""
+        _check(lib().gh_serve_stop(self._h), "serve_stop")
+
     def result(self, q):
         """(state, r0, r1, finish step): SSSP r0 = reachable vertices, r1 = sum
         of their distances; A* r0 = optimal cost (UINT32_MAX unreachable)."""
@@ -106,10 +128,12 @@ def poisson_arrivals(count, rate, seed):
     return np.cumsum(rng.exponential(1.0 / rate, count))
 
 
-def run_stream(server, queries, arrivals, stream=None, max_seconds=600.0):
+def run_stream(server, queries, arrivals, stream=None, max_seconds=600.0, resident=False):
     """Serves `queries` ((kind, dataset, a, b) tuples) arriving at `arrivals`
-    (seconds from the start).  Returns (latency seconds per query, results
-    per query, makespan seconds, steps)."""
+    (seconds from the start), through host steps or, with resident=True,
+    through the device loop (the server must have been started).  Returns
+    (latency seconds per query, results per query, makespan seconds, steps
+    or polls)."""
     n = len(queries)
     ids = [None] * n
     finish = np.full(n, np.nan)
@@ -128,7 +152,7 @@ def run_stream(server, queries, arrivals, stream=None, max_seconds=600.0):
         if done == nxt:  # nothing in the system: wait for the next arrival
             time.sleep(max(0.0, min(arrivals[nxt] - now, 0.001)))
             continue
-        fin, _, _ = server.step(stream)
+        fin, _, _ = server.poll() if resident else server.step(stream)
         steps += 1
         t = time.perf_counter() - t0
         for q in fin:

@@ -343,8 +343,11 @@ gh_status gh_serve_destroy(gh_server* s);
 gh_status gh_serve_set_blocks(gh_server* s, long long vertices_per_block, int sssp_max_blocks, long long cells_per_block,
                               int astar_max_blocks);
 /* Resident datasets; the device arrays stay owned by the caller and must
- * outlive the server.  CSR graph as in gh_sssp; cost grid as in
- * gh_batch_add_astar.  *id gets the dataset index. */
+ * outlive the server.  CSR graph as in gh_sssp (its edge count is read from
+ * rowptr_dev[n], one synchronous copy); cost grid as in gh_batch_add_astar.
+ * *id gets the dataset index.  A query's heap holds max(4 n, m / 2, 16
+ * batches) keys on a graph of n vertices and m edges (the bound of
+ * gh_sssp's heap), 64 keys per side of the larger grid dimension on a map. */
 gh_status gh_serve_add_graph(gh_server* s, int n, const long long* rowptr_dev, const int* col_dev,
                              const unsigned* w_dev, int* id);
 gh_status gh_serve_add_map(gh_server* s, int width, int height, const unsigned char* cost_dev, int* id);
@@ -361,15 +364,43 @@ gh_status gh_serve_submit(gh_server* s, int kind, int dataset, int a, int b, lon
 gh_status gh_serve_step(gh_server* s, void* stream, int* finished, int* active, int* queued);
 /* Results of query `q`: *state 0 queued, 1 admitted, 2 finished, 3 failed;
  * SSSP: r0 = reachable vertices, r1 = sum of their distances; A*: r0 = the
- * optimal cost (UINT32_MAX unreachable), r1 = 0; *finish_step = the step in
- * which it finished.  Any pointer may be NULL. */
+ * optimal cost (UINT32_MAX unreachable), r1 = 0; a failed query: r0 = 0,
+ * r1 = the failure's gh_status; *finish_step = the step in which it
+ * finished.  Any pointer may be NULL. */
 gh_status gh_serve_result(gh_server* s, long long q, int* state, unsigned long long* r0, unsigned long long* r1,
                           long long* finish_step);
 /* Ids of the queries the last step finished (at most max_ids; *count gets
  * how many there were). */
 gh_status gh_serve_finished(gh_server* s, long long* ids, int max_ids, int* count);
-/* Arena bytes in use and free, slots in use, steps run (any may be NULL). */
+/* Arena bytes in use and free, slots in use, steps run (any may be NULL).
+ * With the device loop: steps = launches of the loop. */
 gh_status gh_serve_info(gh_server* s, long long* used_bytes, long long* free_bytes, int* slots_used, long long* steps);
+
+/* The device-resident request loop.  gh_serve_start switches the server to
+ * it (no query may be queued or admitted by gh_serve_step; the loop takes
+ * over the whole arena).  From then on gh_serve_submit writes each query
+ * into a request ring in pinned host memory, and one persistent launch of
+ * the search kernel, on a stream of the server's own, admits requests into
+ * free slots and memory (in arrival order, skipping any that do not fit
+ * yet), resets and seeds their heaps, runs them with `batches_per_step`
+ * batches per block stint, collects the finished ones, frees their memory
+ * and writes their results into a completion ring, with no host step in
+ * between.  The launch leaves after idle_ms (1 .. 600000) with nothing
+ * admitted or waiting, and every wait in it has a limit.  gh_serve_poll
+ * reads the completions (their ids through gh_serve_finished, their
+ * results through gh_serve_result, finish_step = completion order), posts
+ * queries that did not fit into the request ring yet, and launches the loop
+ * again when work is outstanding; it neither synchronizes nor blocks.
+ * *active gets the queries admitted on the device, *queued those not
+ * admitted yet.  gh_serve_stop pauses the loop: the launch leaves after its
+ * blocks' current stints, unfinished queries keep their state, and a later
+ * gh_serve_start resumes them.  GH_ERR_TIMEOUT when a wait of the loop ran
+ * out.  A device-wide synchronization waits for the launch to leave.  The
+ * reference's counterpart is its host relaunch loop (artifacts/astar/
+ * astar_main.cu:127-179). */
+gh_status gh_serve_start(gh_server* s, int idle_ms);
+gh_status gh_serve_poll(gh_server* s, int* finished, int* active, int* queued);
+gh_status gh_serve_stop(gh_server* s);
 
 /* Seeded synthetic cost grid for grid A* (host memory, `threads` host
  * threads): cell i draws r = splitmix64(seed + (i + 1) * golden ratio); it is

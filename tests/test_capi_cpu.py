@@ -62,6 +62,9 @@ def test_rejects_bad_arguments_before_touching_a_device(ghlib):
     assert ghlib.gh_serve_destroy(None) == 1
     assert ghlib.gh_serve_step(None, None, None, None, None) == 1
     assert ghlib.gh_serve_submit(None, 2, 0, 0, 0, None) == 1
+    assert ghlib.gh_serve_start(None, 100) == 1
+    assert ghlib.gh_serve_poll(None, None, None, None) == 1
+    assert ghlib.gh_serve_stop(None) == 1
 
 
 def test_newer_entry_points_reject_bad_arguments(ghlib):

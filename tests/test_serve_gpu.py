@@ -93,7 +93,7 @@ def test_admission_waits_for_memory(datasets, variant, bs):
     graphs, maps = datasets
     qs = make_queries(graphs, maps, 24, 7)
     want = oracle(graphs, maps, qs)
-    s = new_server(graphs, maps, arena_bytes=2 << 20, max_slots=64, batch_size=bs, variant=variant,
+    s = new_server(graphs, maps, arena_bytes=5 << 20, max_slots=64, batch_size=bs, variant=variant,
                    batches_per_step=4)
     try:
         ids = [s.submit(*q) for q in qs]
@@ -145,5 +145,145 @@ def test_edge_queries(datasets):
                 tiny.submit(gs.SSSP, 0, 0)  # can never fit the arena
         finally:
             tiny.close()
+    finally:
+        s.close()
+
+
+# ---------------------------------------------------------------- device loop
+def poll_until_done(s, ids, max_seconds=120.0):
+    """Polls the device loop until every id has completed; returns the peak
+    of `queued` seen."""
+    import time
+    left = set(ids)
+    peak = 0
+    t0 = time.perf_counter()
+    while left:
+        fin, _, queued = s.poll()
+        peak = max(peak, queued)
+        left -= set(fin)
+        assert time.perf_counter() - t0 < max_seconds, f"{len(left)} queries did not complete"
+    return peak
+
+
+def test_device_loop_stream_matches_oracle(datasets):
+    """A Poisson stream through the device-resident loop: every result equals
+    the oracle, and the arena and slots are free at the end."""
+    graphs, maps = datasets
+    qs = make_queries(graphs, maps, 60, 11)
+    want = oracle(graphs, maps, qs)
+    s = new_server(graphs, maps, arena_bytes=1 << 30, max_slots=16, batch_size=256, batches_per_step=2)
+    try:
+        s.start(idle_ms=200)
+        lat, res, makespan, polls = gs.run_stream(s, qs, gs.poisson_arrivals(len(qs), 400.0, 5), resident=True)
+        assert all(r[0] == gs.FINISHED for r in res)
+        assert [(r[1], r[2]) for r in res] == want
+        assert sorted(r[3] for r in res) == list(range(1, len(qs) + 1))  # completion order
+        info = s.info()
+        assert info["used_bytes"] == 0 and info["slots_used"] == 0 and info["steps"] >= 1
+        with pytest.raises(Exception):
+            s.step()  # host steps are off once the device loop runs
+    finally:
+        s.close()
+
+
+@pytest.mark.parametrize("variant,bs", [("topdown", 128), ("bottomup", 512)])
+def test_device_loop_admission_waits_for_memory(datasets, variant, bs):
+    """An arena that holds about two of the largest queries: the device
+    admits the rest as memory frees up, in arrival order where they fit."""
+    graphs, maps = datasets
+    qs = make_queries(graphs, maps, 24, 7)
+    want = oracle(graphs, maps, qs)
+    s = new_server(graphs, maps, arena_bytes=5 << 20, max_slots=64, batch_size=bs, variant=variant,
+                   batches_per_step=4)
+    try:
+        s.start(idle_ms=200)
+        ids = [s.submit(*q) for q in qs]
+        peak = poll_until_done(s, ids)
+        res = [s.result(q) for q in ids]
+        assert [(r[1], r[2]) for r in res] == want
+        assert peak > 0  # memory, not slots, held some back
+        assert s.info()["used_bytes"] == 0
+    finally:
+        s.close()
+
+
+def test_device_loop_idle_exit_relaunch_and_stop(datasets):
+    """The loop's launch leaves after its idle limit and poll() launches it
+    again for new work; stop() pauses it mid-stream and start() resumes the
+    queries it left, all results exact."""
+    import time
+    graphs, maps = datasets
+    qs = make_queries(graphs, maps, 40, 21)
+    want = oracle(graphs, maps, qs)
+    s = new_server(graphs, maps, arena_bytes=1 << 30, max_slots=8, batch_size=256, batches_per_step=1)
+    try:
+        s.start(idle_ms=5)
+        a = s.submit(*qs[0])
+        poll_until_done(s, [a])
+        time.sleep(0.2)  # well past the idle limit: the launch has left
+        s.poll()
+        first = s.info()["steps"]
+        b = s.submit(*qs[1])
+        poll_until_done(s, [b])
+        assert s.info()["steps"] == first + 1
+        rest = [s.submit(*q) for q in qs[2:]]
+        for _ in range(3):
+            s.poll()
+        s.stop()
+        time.sleep(0.05)
+        fin, _, _ = s.poll()  # paused: collects what completed, launches nothing
+        steps = s.info()["steps"]
+        time.sleep(0.05)
+        assert s.poll()[0] == [] and s.info()["steps"] == steps
+        pending = [q for q in rest if s.result(q)[0] not in (gs.FINISHED, gs.FAILED)]
+        assert pending  # the pause left work in the loop
+        s.start()
+        poll_until_done(s, pending)
+        ids = [a, b] + rest
+        res = [s.result(q) for q in ids]
+        assert all(r[0] == gs.FINISHED for r in res)
+        assert [(r[1], r[2]) for r in res] == want
+    finally:
+        s.close()
+
+
+def test_device_loop_edge_queries(datasets):
+    """Start == goal, a blocked start cell and an isolated vertex through the
+    device loop."""
+    graphs, maps = datasets
+    g = gsssp.rmat_graph(10, 8, seed=3)
+    rowptr = g.host()[0]
+    iso = np.nonzero(np.diff(rowptr) == 0)[0]
+    blocked = gb.gen_grid(40, 9)
+    blocked[0, 0] = 0
+    s = gs.Server(arena_bytes=256 << 20, max_slots=8, batch_size=64)
+    try:
+        gi = s.add_graph(g)
+        mi = s.add_map(torch.from_numpy(maps[0]).cuda())
+        bi = s.add_map(torch.from_numpy(blocked).cuda())
+        s.start(idle_ms=50)
+        qs = [(gs.ASTAR, mi, 5, 5), (gs.ASTAR, bi, 0, blocked.size - 1)]
+        if iso.size:
+            qs.append((gs.SSSP, gi, int(iso[0]), 0))
+        ids = [s.submit(*q) for q in qs]
+        poll_until_done(s, ids)
+        res = [s.result(q) for q in ids]
+        assert res[0][:3] == (gs.FINISHED, 0, 0)
+        assert res[1][:3] == (gs.FINISHED, 0xFFFFFFFF, 0)
+        if iso.size:
+            assert res[2][:3] == (gs.FINISHED, 1, 0)
+    finally:
+        s.close()
+
+
+def test_device_loop_needs_an_idle_server(datasets):
+    graphs, maps = datasets
+    s = new_server(graphs, maps, arena_bytes=64 << 20, max_slots=4, batch_size=64)
+    try:
+        s.submit(gs.ASTAR, len(graphs), 0, 1)
+        with pytest.raises(Exception):
+            s.start()  # a query waits for a host step
+        with pytest.raises(Exception):
+            s.poll()  # not started
     finally:
         s.close()
