@@ -191,7 +191,7 @@ __device__ __forceinline__ void flush_full(const H& heap, u64* emit, int* cnt, i
     __syncthreads();
     const int c = *cnt;
     if (c >= B) {
-        heap.insertion(reinterpret_cast<typename H::key_type*>(emit), B, heapOff);
+        gh::app::insert_keys(heap, emit, B, heapOff);
         for (int i = threadIdx.x; i < c - B; i += blockDim.x) emit[i] = emit[B + i];
         __syncthreads();
         if (threadIdx.x == 0) *cnt = c - B;
@@ -204,7 +204,7 @@ template <typename H>
 __device__ __forceinline__ void flush_rest(const H& heap, u64* emit, int* cnt, int heapOff, unsigned long long& inserted) {
     __syncthreads();
     const int c = *cnt;
-    if (c > 0) heap.insertion(reinterpret_cast<typename H::key_type*>(emit), c, heapOff);
+    if (c > 0) gh::app::insert_keys(heap, emit, c, heapOff);
     inserted += c;
     __syncthreads();
     if (threadIdx.x == 0) *cnt = 0;
@@ -273,7 +273,7 @@ __device__ void fifo_to_heap(const H& heap, const gh::Fifo<u64>& f, u64* batch, 
         f.copy_out(c, batch);
         f.release(c);
         __syncthreads();
-        heap.insertion(reinterpret_cast<typename H::key_type*>(batch), c.n, heapOff);
+        gh::app::insert_keys(heap, batch, c.n, heapOff);
         if (heap.failed()) break;
     }
 }
@@ -299,7 +299,7 @@ __device__ bool run_astar(const H& heap, Inst* in, unsigned char* smem, int heap
         if (maxBatches && batches++ == maxBatches) { over = false; break; }
         if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
         int size = 0;
-        heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap), heapOff);
+        size = gh::app::take_batch(heap, batch, prune(heap), heapOff);
         pops += size;
         for (int base = 0; base < size; base += T) {
             const int i = base + tid;
@@ -381,7 +381,7 @@ __device__ bool run_knapsack(const H& heap, Inst* in, unsigned char* smem, int h
         int size = 0;
         if (mode == 0) {
             if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart, prune)) break;
-            heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, prune(heap), heapOff);
+            size = gh::app::take_batch(heap, batch, prune(heap), heapOff);
         } else {
             // breadth-first (models_fifo.cuh:46-52): the oldest batch of the ring;
             // the search is over when the ring is empty (one block owns it)
@@ -500,7 +500,7 @@ __device__ bool run_sssp(const H& heap, Inst* in, unsigned char* smem, int heapO
         if (maxBatches && batches++ == maxBatches) { over = false; break; }
         if (gh::app::wait_for_keys(heap, &ctl[2], &in->stop, lastBusy, waitStart)) break;
         int size = 0;
-        heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, heapOff);
+        size = gh::app::take_batch(heap, batch, heapOff);
         pops += size;
         if (size > 0)
             gh::app::sssp_relax_batch(heap, batch, size, pre, wsum, emit, &ctl[1], in->rowptr, in->col, in->wt, in->g,

@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(1024) k_sssp(H heap, const long long* __restri
     if (blockIdx.x == 0 && source >= 0) {
         if (tid == 0) emit[0] = static_cast<u64>(source);  // distance 0
         __syncthreads();
-        heap.insertion(reinterpret_cast<typename H::key_type*>(emit), 1, heapOff);
+        gh::app::insert_keys(heap, emit, 1, heapOff);
         __syncthreads();
         gh::app::batch_done(st);
     }
@@ -103,8 +103,7 @@ __global__ void __launch_bounds__(1024) k_sssp(H heap, const long long* __restri
     int lastBusy = -1;
     for (;;) {
         if (gh::app::wait_for_keys(heap, &ctl[2], nullptr, lastBusy, waitStart)) break;
-        int size = 0;
-        heap.deleteMin(reinterpret_cast<typename H::key_type*>(batch), size, heapOff);
+        const int size = gh::app::take_batch(heap, batch, heapOff);
         if (size == 0) {  // another block took the last keys first
             gh::app::batch_done(st);
             if (heap.failed()) break;

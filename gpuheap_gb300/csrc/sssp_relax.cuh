@@ -10,6 +10,7 @@
 // inserts full batches as they form; the remainder is inserted at the end.
 #pragma once
 #include "gpuheap_device.cuh"
+#include "worklist.cuh"
 
 namespace gh {
 namespace app {
@@ -90,7 +91,7 @@ __device__ __forceinline__ void sssp_relax_batch(const H& heap, const unsigned l
         __syncthreads();
         const int c = *cnt;
         if (c >= B) {
-            heap.insertion(reinterpret_cast<const typename H::key_type*>(emit), B, heapOff);
+            insert_keys(heap, emit, B, heapOff);
             for (int i = tid; i < c - B; i += T) emit[i] = emit[B + i];
             __syncthreads();
             if (tid == 0) *cnt = c - B;
@@ -99,7 +100,7 @@ __device__ __forceinline__ void sssp_relax_batch(const H& heap, const unsigned l
         __syncthreads();
     }
     const int rest = *cnt;
-    if (rest > 0) heap.insertion(reinterpret_cast<const typename H::key_type*>(emit), rest, heapOff);
+    if (rest > 0) insert_keys(heap, emit, rest, heapOff);
     inserted += rest;
     __syncthreads();
     if (tid == 0) *cnt = 0;

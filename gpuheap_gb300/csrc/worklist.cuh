@@ -18,6 +18,32 @@
 namespace gh {
 namespace app {
 
+// Heap calls of the search loops, kept out of line.  Inlined into a search
+// loop, insertion and deleteMin (with their merges) compete for registers
+// with the loop's own state, and the compiler spills inside the merge
+// loops; as calls, the heap code has the registers to itself and a call
+// saves and restores a few of the caller's.
+template <typename H>
+__device__ __noinline__ void insert_keys(H heap, const unsigned long long* keys, int n, int heapOff) {
+    heap.insertion(reinterpret_cast<const typename H::key_type*>(keys), n, heapOff);
+}
+
+// deleteRoot with a prune threshold (keys at or above it stay); returns the
+// number of keys taken.
+template <typename H>
+__device__ __noinline__ int take_batch(H heap, unsigned long long* out, typename H::key_type threshold, int heapOff) {
+    int size = 0;
+    heap.deleteMin(reinterpret_cast<typename H::key_type*>(out), size, threshold, heapOff);
+    return size;
+}
+
+template <typename H>
+__device__ __noinline__ int take_batch(H heap, unsigned long long* out, int heapOff) {
+    int size = 0;
+    heap.deleteMin(reinterpret_cast<typename H::key_type*>(out), size, heapOff);
+    return size;
+}
+
 // No prune threshold: every key is worth taking.
 struct NoThreshold {
     template <typename H>
