@@ -25,6 +25,11 @@ modelled here at the level of those atomic steps:
 * termination of a search (gpuheap_gb300/csrc/worklist.cuh): blocks that
   share one heap count themselves busy while they hold work; the search
   must end exactly when the work is done, with no block left waiting.
+* the retrieving heap's steal (include/gpuheap_retrieve.cuh; reference
+  applications/sssp_longfei_new/heap.cuh:20-35, 147-199, 338-380): a
+  retrieve that needs the last node while an insert is still on its way
+  down to it takes the insert's batch through the root instead, by the
+  per-node word is_taken (0 -> 1 -> 2 -> 3 -> 0).
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -370,6 +375,109 @@ def termination_model(blocks=2, depth=2, count_while_waiting=False):
             raise Violation(f"search ended with heap {g.heap}, busy {g.busy}, {g.processed}/{total} units", trace)
 
     return (TermState(heap=(depth,), busy=0, processed=0), tuple(["wait"] * blocks)), actors, final
+
+
+# --------------------------------------------------------------------------
+# the retrieving heap: a retrieve takes the target of an insert in flight
+
+StealState = namedtuple("StealState", "t_lock taken t_batch root got")
+T_FREE, T_INS, T_RET = 0, 1, 2
+
+
+def retrieve_steal_model(path_steps=2, lock_before_check=True, retrieve_locks_target=True, root_before_signal=True):
+    """One insert on its way down to its target t (`path_steps` nodes of its
+    path still ahead, t the last; it set is_taken[t] = 1 when it started)
+    and one retrieve that holds the root's lock and wants t as the last node.
+
+    * `ins` holds the lock of its current node; a step locks the next node
+      on the path, releases the current one, then reads is_taken[t]: 2 means
+      a retrieve took t, so it releases the node it holds, writes its batch
+      into the root (whose lock the retrieve holds) and sets is_taken[t] = 3.
+      Reaching t, it writes t, sets is_taken[t] = 0 and releases t.
+    * `ret` locks t and reads is_taken[t]: 0, t holds a batch: read it; 1,
+      an insert is on its way: set 2, release t, wait for 3, set 0 and read
+      the root.
+
+    got counts the retrieve's receipts of the insert's batch: 1 at the end.
+    Planted mistakes: the insert reads is_taken before it locks the next
+    node, the retrieve reads and sets is_taken without locking t, or the
+    insert signals 3 before it has written the root."""
+
+    def ins(g, pc, trace):
+        if isinstance(pc, tuple) and pc[0] == "at":  # holds node k's lock
+            k = pc[1]
+            nxt = k + 1
+            if not lock_before_check:
+                return [(f"reads is_taken before locking node {nxt}", g, ("late_lock", nxt, g.taken == 2))]
+            if nxt == path_steps:  # the target
+                if g.t_lock != T_FREE:
+                    return []
+                return [("locks t, releases its node", _set(g, t_lock=T_INS), ("check", nxt))]
+            return [(f"locks node {nxt}, releases node {k}", g, ("check", nxt))]
+        if isinstance(pc, tuple) and pc[0] == "late_lock":
+            _, nxt, abandon = pc
+            if nxt == path_steps:
+                if g.t_lock != T_FREE:
+                    return []
+                g = _set(g, t_lock=T_INS)
+            if abandon:
+                return [("abandons (read earlier)", _set(g, t_lock=T_FREE) if nxt == path_steps else g, "write_root")]
+            return [(f"holds node {nxt}", g, "write_t" if nxt == path_steps else ("at", nxt))]
+        if isinstance(pc, tuple) and pc[0] == "check":
+            j = pc[1]
+            if g.taken == 2:
+                return [("sees 2: releases its node", _set(g, t_lock=T_FREE) if j == path_steps else g, "write_root")]
+            return [("no steal", g, "write_t" if j == path_steps else ("at", j))]
+        if pc == "write_t":
+            if g.t_lock != T_INS:
+                raise Violation("insert writes t without holding it", list(trace) + ["ins:write_t"])
+            return [("writes t, is_taken 0, releases t", _set(g, t_batch=True, taken=0, t_lock=T_FREE), None)]
+        if pc == "write_root":
+            if root_before_signal:
+                return [("writes the root", _set(g, root=True), "signal")]
+            return [("sets is_taken 3 first", _set(g, taken=3), "late_root")]
+        if pc == "signal":
+            return [("is_taken 2 -> 3", _set(g, taken=3), None)]
+        if pc == "late_root":
+            return [("writes the root", _set(g, root=True), None)]
+        return []
+
+    def ret(g, pc, trace):
+        if pc == "lock_t":
+            if not retrieve_locks_target:
+                return [("reads is_taken without the lock", g, "read_taken")]
+            if g.t_lock != T_FREE:
+                return []
+            return [("locks t", _set(g, t_lock=T_RET), "read_taken")]
+        if pc == "read_taken":
+            if g.taken == 0:
+                return [("is_taken 0: t is a node", g, "read_t")]
+            if g.taken == 1:
+                return [("is_taken 1 -> 2", _set(g, taken=2), "release")]
+            raise Violation(f"retrieve found is_taken {g.taken}", list(trace) + ["ret:read_taken"])
+        if pc == "read_t":
+            if not g.t_batch:
+                raise Violation("retrieve read t before the insert wrote it", list(trace) + ["ret:read_t"])
+            g = _set(g, got=g.got + 1, t_batch=False)
+            return [("reads t, releases t", _set(g, t_lock=T_FREE) if g.t_lock == T_RET else g, None)]
+        if pc == "release":
+            return [("releases t", _set(g, t_lock=T_FREE) if g.t_lock == T_RET else g, "wait3")]
+        if pc == "wait3":
+            return [("sees 3, sets 0", _set(g, taken=0), "read_root")] if g.taken == 3 else []
+        if pc == "read_root":
+            if not g.root:
+                raise Violation("retrieve read the root before the insert wrote it", list(trace) + ["ret:read_root"])
+            return [("reads the root", _set(g, got=g.got + 1, root=False), None)]
+        return []
+
+    def final(g, trace):
+        if g.got != 1 or g.root or g.t_batch:
+            raise Violation(f"batch received {g.got} times (root {g.root}, t {g.t_batch})", trace)
+        if g.taken != 0 or g.t_lock != T_FREE:
+            raise Violation(f"t left with is_taken {g.taken}, lock {g.t_lock}", trace)
+
+    g0 = StealState(t_lock=T_FREE, taken=1, t_batch=False, root=False, got=0)
+    return (g0, (("at", 0), "lock_t")), [ins, ret], final
 
 
 # --------------------------------------------------------------------------

@@ -14,7 +14,7 @@ scenario), `large` (bgpq_ref_cases_large.npz, batch 256-2048, the batch
 sizes of the heap-sort configurations) and `retrieve`
 (retrieve_ref_cases.npz: insert / retrieve sequences through the reference's
 retrieving heap, applications/sssp_longfei_new/heap.cuh, pinning the runs
-that `retrieve` returns).
+that `retrieve` returns and the heap each sequence leaves).
 
 Usage (needs the reference tree; not run by the tests):
     make -C oracle ref REF=<reference tree> && python tests/golden/make_golden.py [small] [large] [retrieve]
@@ -211,21 +211,35 @@ def run_retrieve_case(ref, kind, B, seed, rng, n_ops):
             taken.append(sz.value)
             runs.append(out[:sz.value].copy())
             held -= sz.value
+    # the heap at the end: its valid nodes, the valid part of its partial
+    # buffer and {curr_batch_count, curr_pb_size}
+    items = np.zeros(bn * B, dt)
+    pb = np.zeros(B, dt)
+    counters = np.zeros(2, np.int32)
+    f("state")(VP(h), VP(items.ctypes.data), VP(pb.ctypes.data), VP(counters.ctypes.data))
     f("destroy", None)(VP(h))
     arrays = dict(ops=np.asarray(ops, np.int32), keys=np.concatenate(keys) if keys else np.zeros(0, dt),
-                  taken=np.asarray(taken, np.int32), runs=np.concatenate(runs) if runs else np.zeros(0, dt))
-    meta = dict(key=kind, batch_size=B, seed=seed, ties=ties)
+                  taken=np.asarray(taken, np.int32), runs=np.concatenate(runs) if runs else np.zeros(0, dt),
+                  final_nodes=items[:int(counters[0]) * B].copy(), final_pb=pb[:int(counters[1])].copy(),
+                  final_counters=counters)
+    meta = dict(key=kind, batch_size=B, seed=seed, ties=ties, batch_num=bn)
     return arrays, meta
 
 
 def retrieve_cases():
-    """12 sequences of inserts and retrievals: {u32, u64} x batch {16, 64,
-    256} x two seeds (every third seed draws keys from ~40 values)."""
+    """16 sequences of inserts and retrievals: {u32, u64} x batch {16, 64,
+    256} x two seeds (every third seed draws keys from ~40 values), then four
+    longer u64 sequences at batch 32 and 128 (a deeper heap, every branch of
+    retrieve's refill taken many times)."""
     for kind in ("u32", "u64"):
         for B in (16, 64, 256):
             for k in range(2):
                 seed = 9000 + 31 * B + 7 * k + (0 if kind == "u32" else 1)
                 yield kind, B, seed, np.random.default_rng(seed), 160
+    for B in (32, 128):
+        for k in range(2):
+            seed = 9500 + 13 * B + k
+            yield "u64", B, seed, np.random.default_rng(seed), 300
 
 
 def _fn_rr(lib, kind, name, res):

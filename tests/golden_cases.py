@@ -51,7 +51,10 @@ def _retrieve_data():
 
 def retrieve_case(i):
     """ops (positive: insert that many of `keys` in order; negative: retrieve
-    -op keys), taken (each retrieve's count), runs (retrieved keys, joined)."""
+    -op keys), taken (each retrieve's count), runs (retrieved keys, joined),
+    final_nodes / final_pb / final_counters (the reference heap's valid nodes,
+    valid partial buffer and {batch count, pb size} after the sequence), and
+    the meta fields (key, batch_size, batch_num, seed, ties)."""
     d = _retrieve_data()
     p = f"c{i}_"
     out = {k[len(p):]: d[k] for k in d.files if k.startswith(p)}

@@ -143,3 +143,19 @@ def test_waiting_for_the_parent_without_parking_deadlocks():
     assert r.deadlocks and r.deadlocks[0] == ["holder:sift toward x", "ins:cas p fail; wait holding x"]
     r = _run(lm.bottomup_park_model(park_before_wait=False, with_taker=False, with_passer=False))
     assert not r.deadlocks and r.finals == 1
+
+
+# ------------------------------------------------------ retrieving heap steal
+@pytest.mark.parametrize("steps", [1, 2, 3])
+def test_retrieve_steal_is_safe(steps):
+    res = _run(lm.retrieve_steal_model(path_steps=steps))
+    assert res.deadlocks == [] and res.finals > 0
+
+
+@pytest.mark.parametrize("mistake", ["lock_before_check", "retrieve_locks_target", "root_before_signal"])
+def test_retrieve_steal_planted_mistakes_are_caught(mistake):
+    try:
+        res = _run(lm.retrieve_steal_model(path_steps=2, **{mistake: False}))
+    except lm.Violation:
+        return
+    assert res.deadlocks, f"{mistake}: no violation and no deadlock found"
