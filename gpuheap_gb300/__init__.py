@@ -67,6 +67,16 @@ _SIGS = {
     "gh_rmat_edges": (_I, [_I, _LL, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong,
                            ctypes.c_uint, _VP, _VP, _VP, _VP]),
     "gh_sssp": (_I, [_VP, _I, _VP, _VP, _VP, _I, _VP, _VP, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "gh_rheap_create": (_I, [ctypes.POINTER(_VP), _I, _I, _I, _VP]),
+    "gh_rheap_destroy": (_I, [_VP]),
+    "gh_rheap_reset": (_I, [_VP, _VP]),
+    "gh_rheap_set_timeout": (_I, [_VP, ctypes.c_double]),
+    "gh_rheap_insert": (_I, [_VP, _VP, _I, _VP]),
+    "gh_rheap_retrieve": (_I, [_VP, _VP, ctypes.POINTER(_I), _VP]),
+    "gh_rheap_concurrent": (_I, [_VP, _VP, _LL, _I, _I, _I, _I, _VP, _LL, _VP, _I, ctypes.POINTER(_LL),
+                                 ctypes.POINTER(_I), _VP]),
+    "gh_rheap_state": (_I, [_VP, _VP, _VP, _VP]),
+    "gh_sssp_retrieve": (_I, [_I, _VP, _VP, _VP, _I, _VP, _I, _I, _I, _LL, _VP, ctypes.POINTER(ctypes.c_ulonglong)]),
     "gh_heap_view_bytes": (ctypes.c_size_t, []),
     "gh_heap_device_view": (_I, [_VP, _VP, ctypes.c_size_t]),
     "gh_heap_smem_bytes": (ctypes.c_size_t, [_I, _I]),

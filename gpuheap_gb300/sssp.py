@@ -85,3 +85,20 @@ def sssp(heap, graph, source, dist=None, stream=None):
     _check(lib().gh_sssp(heap._h, graph.n, graph.rowptr.data_ptr(), graph.col.data_ptr(), graph.w.data_ptr(),
                          int(source), dist.data_ptr(), s, stats), "sssp")
     return dist, {"keys_taken": stats[0], "edges_scanned": stats[1], "keys_inserted": stats[2]}
+
+
+def sssp_retrieve(graph, source, batch_size=256, chunk=32, blocks=32, capacity_keys=0, dist=None, stream=None):
+    """SSSP through the retrieving heap with the auxiliary buffer
+    (gh_sssp_retrieve; the reference's ssspKernel,
+    applications/sssp_longfei_new/sssp.cu:19-132).  Returns (distances as
+    u32 bits in an int32 tensor, {keys_taken, edges, keys_inserted,
+    handovers})."""
+    import torch
+    if dist is None:
+        dist = torch.empty(graph.n, dtype=torch.int32, device=graph.col.device)
+    stats = (ctypes.c_ulonglong * 4)()
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    _check(lib().gh_sssp_retrieve(graph.n, graph.rowptr.data_ptr(), graph.col.data_ptr(), graph.w.data_ptr(),
+                                  int(source), dist.data_ptr(), int(batch_size), int(chunk), int(blocks),
+                                  int(capacity_keys), s, stats), "sssp_retrieve")
+    return dist, {"keys_taken": stats[0], "edges": stats[1], "keys_inserted": stats[2], "handovers": stats[3]}

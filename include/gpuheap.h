@@ -243,6 +243,67 @@ gh_status gh_sssp(gh_heap* h, int n, const long long* rowptr_dev, const int* col
                   int source, unsigned* dist_dev, void* stream, unsigned long long* stats_host);
 
 /* ------------------------------------------------------------------------
+ * The retrieving heap of the reference's SSSP application
+ * (applications/sssp_longfei_new/heap.cuh, heap_with_aux.cuh): 0-based nodes,
+ * a separate partial buffer, top-down inserts, and retrieve(), which takes
+ * the `size` smallest keys and refills the root in place -- from the partial
+ * buffer or the last node, or, when an insert is still on its way down to
+ * the last node, from that insert's batch handed over through the root (the
+ * is_taken protocol).  Device code: include/gpuheap_retrieve.cuh
+ * (gh::RetHeap<K>, gh::RetHeapAux<K, Aux>).  Keys u32 or u64; batch_size a
+ * power of two in [16, 2048]; every operation is one thread block.
+ * ------------------------------------------------------------------------ */
+typedef struct gh_rheap gh_rheap;
+
+/* Heap<T>(batch_num, batch_size, init_limit) (heap.cuh:56-64): init_limit
+ * points to one key of the kind (NULL = its maximum).  Synchronizes. */
+gh_status gh_rheap_create(gh_rheap** out, int key_kind, int batch_num, int batch_size, const void* init_limit);
+gh_status gh_rheap_destroy(gh_rheap* h);
+/* Empties the heap (nodes and partial buffer to init_limit, counters, lock
+ * and is_taken words to zero). */
+gh_status gh_rheap_reset(gh_rheap* h, void* stream);
+/* Time limit of every device-side wait, in (0, 60] seconds (default 2 s). */
+gh_status gh_rheap_set_timeout(gh_rheap* h, double seconds);
+/* insert(items, count) (heap.cuh:272-382) by one thread block; 0 <= count
+ * <= batch_size.  A full heap (batch count >= batch_num - 1) takes nothing
+ * and records GH_ERR_CAPACITY (gh_rheap_state counters[2]); the reference
+ * flags need_gc and drops the keys. */
+gh_status gh_rheap_insert(gh_rheap* h, const void* keys_dev, int count, void* stream);
+/* retrieve(ret, *size) (heap.cuh:79-270) by one thread block: *size in:
+ * keys wanted; out: keys written to out_dev, the smallest held, ascending
+ * (at most batch_size).  Synchronizes the stream. */
+gh_status gh_rheap_retrieve(gh_rheap* h, void* out_dev, int* size, void* stream);
+/* One launch of inserters + retrievers blocks: the first insert keys_dev[0,
+ * n) in chunks of `chunk` keys, the others retrieve `size` keys at a time
+ * until the inserters are done and the heap is empty.  Retrieved runs are
+ * appended to out_dev (at most max_out keys); runs_dev[2r], runs_dev[2r+1]
+ * = start and length of run r (at most max_runs).  *n_out, *n_runs: keys and
+ * runs retrieved.  GH_ERR_CAPACITY when out_dev or runs_dev were too small.
+ * Synchronizes the stream.  It has no counterpart in the reference: it is
+ * the concurrent test of the is_taken hand-over. */
+gh_status gh_rheap_concurrent(gh_rheap* h, const void* keys_dev, long long n, int chunk, int inserters, int retrievers,
+                              int size, void* out_dev, long long max_out, int* runs_dev, int max_runs,
+                              long long* n_out, int* n_runs, void* stream);
+/* Host copies: items_host (batch_num * batch_size keys), pb_host (batch_size
+ * keys), counters_host[6] = {batch count, partial-buffer size, device error,
+ * retrieves that took an insert's batch through the root, inserts refused
+ * as full, error site}; any pointer may be NULL.  Synchronizes the device. */
+gh_status gh_rheap_state(gh_rheap* h, void* items_host, void* pb_host, long long* counters_host);
+/* SSSP through the retrieving heap with the auxiliary buffer (the reference's
+ * ssspKernel, applications/sssp_longfei_new/sssp.cu:19-132): `blocks` blocks
+ * each retrieve up to batch_size keys with their edge offsets, relax at most
+ * `chunk` edges of each current key, put keys with edges left back into the
+ * buffer, and insert the improved vertices.  The search ends by the
+ * busy-counter protocol (the reference's term_sig check, sssp.cu:58-70, can
+ * end while a block still inserts).  A heap of capacity_keys (0: max(4 n,
+ * m / 2) + 16 batches) keys is allocated for the call.  CSR graph and
+ * distances as in gh_sssp.  stats_host (may be NULL): {keys taken, edges
+ * relaxed, keys inserted, hand-overs through the root}.  Synchronizes. */
+gh_status gh_sssp_retrieve(int n, const long long* rowptr_dev, const int* col_dev, const unsigned* w_dev, int source,
+                           unsigned* dist_dev, int batch_size, int chunk, int blocks, long long capacity_keys,
+                           void* stream, unsigned long long* stats_host);
+
+/* ------------------------------------------------------------------------
  * Batched searches: many independent grid A* and 0/1 knapsack instances of
  * uneven size, each with its own heap (u64 keys, partial buffer), run by one
  * persistent launch.  The reference runs one search per process and launch

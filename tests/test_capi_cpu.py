@@ -62,6 +62,12 @@ def test_rejects_bad_arguments_before_touching_a_device(ghlib):
     assert ghlib.gh_serve_destroy(None) == 1
     assert ghlib.gh_serve_step(None, None, None, None, None) == 1
     assert ghlib.gh_serve_submit(None, 2, 0, 0, 0, None) == 1
+    assert ghlib.gh_rheap_create(None, 2, 64, 64, None) == 1
+    assert ghlib.gh_rheap_destroy(None) == 1
+    assert ghlib.gh_rheap_insert(None, None, 1, None) == 1
+    assert ghlib.gh_rheap_retrieve(None, None, None, None) == 1
+    assert ghlib.gh_rheap_state(None, None, None, None) == 1
+    assert ghlib.gh_sssp_retrieve(0, None, None, None, 0, None, 64, 8, 1, 0, None, None) == 1
     assert ghlib.gh_serve_start(None, 100) == 1
     assert ghlib.gh_serve_poll(None, None, None, None) == 1
     assert ghlib.gh_serve_stop(None) == 1
