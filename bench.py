@@ -92,6 +92,8 @@ def parse():
     p.add_argument("--scale", type=int, default=22, help="sssp: R-MAT scale")
     p.add_argument("--sources", type=int, default=32, help="sssp: seeded random sources (one per step)")
     p.add_argument("--cpu-sources", type=int, default=16, help="sssp: sources in the CPU Dijkstra sample")
+    p.add_argument("--retrieve-sources", type=int, default=4,
+                   help="sssp: sources also run through the retrieving heap (gh_sssp_retrieve); 0 skips it")
     args = p.parse_args()
     if args.workload == "sssp":
         if "--steps" not in sys.argv:
@@ -547,6 +549,33 @@ def sssp_arm(args):
         "scanned_edges_per_source": round(edges / args.steps), "keys_taken_per_source": round(keys / args.steps),
         "gpu_launches": launches, "clocks": clk.summary(),
     }
+    # the reference application's own form: the retrieving heap with the
+    # auxiliary buffer (gh_sssp_retrieve), at the reference's configuration
+    # (batch 512, 256-edge chunks, 10 blocks: sssp_config.cuh) and at batch
+    # 1024 with 64-edge chunks on 24 blocks; each call allocates its heap
+    if args.retrieve_sources > 0:
+        forms = {}
+        k = min(args.retrieve_sources, args.steps)
+        for name, (bsz, chunk, blocks) in (("reference_config", (512, 256, 10)), ("b1024_c64_x24", (1024, 64, 24))):
+            gs.sssp_retrieve(g, int(srcs[0]), batch_size=bsz, chunk=chunk, blocks=blocks)  # warm-up
+            times, same = [], True
+            for i in range(k):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                d2, st2 = gs.sssp_retrieve(g, int(srcs[i]), batch_size=bsz, chunk=chunk, blocks=blocks)
+                e1.record()
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+                if i < len(dists):
+                    same = same and bool(np.array_equal(d2.cpu().numpy().view(np.uint32), dists[i]))
+            if not same:
+                raise SystemExit("bench: SSSP through the retrieving heap differs from gh_sssp")
+            forms[name] = {"batch_size": bsz, "chunk": chunk, "blocks": blocks,
+                           "ms_per_source": round(statistics.mean(times), 2),
+                           "handovers_last_source": st2["handovers"]}
+        line["retrieving_heap_form"] = dict(forms, sources=k, note="gh_sssp_retrieve (the reference's ssspKernel "
+                                            "on its retrieving heap with the auxiliary buffer); distances equal "
+                                            "gh_sssp's; each call allocates its heap")
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         k = min(args.cpu_sources, args.steps)
