@@ -180,10 +180,46 @@ struct SsspRetSmem {
                            + static_cast<size_t>(B) * 8    // current keys
                            + static_cast<size_t>(B + 1) * 8  // edge prefix
                            + static_cast<size_t>(B) * 4    // current keys' offsets
-                           + 64;                           // control words
+                           + 64                            // control words
+                           + 32 * 8;                       // warp sums of the scan
         return (raw + 15) / 16 * 16;
     }
 };
+
+// In-place inclusive prefix sum of x[0, n) over the block (a chunk of
+// consecutive entries per thread, warp shuffles, then the warp totals);
+// wsum: 32 shared slots.  Ends with a barrier.
+__device__ void block_inclusive_scan(long long* x, int n, long long* wsum) {
+    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int per = (n + T - 1) / T;
+    long long local = 0;
+    for (int j = 0; j < per; ++j) {
+        const int i = tid * per + j;
+        if (i < n) local += x[i];
+    }
+    long long incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        long long v = lane < (T >> 5) ? wsum[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        wsum[lane] = v;
+    }
+    __syncthreads();
+    long long run = incl - local + (warp ? wsum[warp - 1] : 0);
+    for (int j = 0; j < per; ++j) {
+        const int i = tid * per + j;
+        if (i < n) { run += x[i]; x[i] = run; }
+    }
+    __syncthreads();
+}
 
 // ssspKernel (sssp.cu:19-132) on the retrieving heap with the auxiliary
 // buffer: each block takes up to B keys, keeps those still current, relaxes
@@ -204,6 +240,7 @@ __global__ void __launch_bounds__(1024) k_sssp_retrieve(gh::RetHeapAux<u64, int>
     long long* pre = reinterpret_cast<long long*>(cur + B);
     int* curOff = reinterpret_cast<int*>(pre + B + 1);
     int* ctl = curOff + B;  // 16 words
+    long long* wsum = reinterpret_cast<long long*>(ctl + 16);  // 32 warp sums
     const int heapOff = static_cast<int>(SsspRetSmem::bytes(B));
     u64* emit = emitAll + static_cast<size_t>(blockIdx.x) * B * chunk;
     gh::HeapState* st = h.heap.state;
@@ -257,19 +294,19 @@ __global__ void __launch_bounds__(1024) k_sssp_retrieve(gh::RetHeapAux<u64, int>
         }
         __syncthreads();
         const int nc = ctl[1];
+        // edges of each current key, then their exclusive prefix in pre[0, nc]
+        for (int j = tid; j < nc; j += T) {
+            const int v = static_cast<int>(cur[j] & 0xffffffffu);
+            long long e = rowptr[v + 1] - rowptr[v] - curOff[j];
+            if (e > chunk) e = chunk;
+            pre[j + 1] = e > 0 ? e : 0;
+        }
         if (tid == 0) {
-            long long run = 0;
-            for (int j = 0; j < nc; ++j) {
-                pre[j] = run;
-                const int v = static_cast<int>(cur[j] & 0xffffffffu);
-                long long e = rowptr[v + 1] - rowptr[v] - curOff[j];
-                if (e > chunk) e = chunk;
-                run += e > 0 ? e : 0;
-            }
-            pre[nc] = run;
+            pre[0] = 0;
             ctl[2] = 0;
         }
         __syncthreads();
+        block_inclusive_scan(pre + 1, nc, wsum);
         const long long total = pre[nc];
         edges += total;
         for (long long ei = tid; ei < total; ei += T) {
