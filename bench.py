@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--owner-depth", type=int, default=-1,
                    help="owner-mode bulk delete: resident depth 2..4, 0 off, -1 automatic")
     p.add_argument("--threads", type=int, default=0, help="threads per block (0: automatic)")
+    p.add_argument("--tune", action="store_true",
+                   help="heapsort: pick batch size, layout, threads, blocks and owner depth with the autotuner "
+                        "(gpuheap_gb300.tune) on a 2^22 sample first")
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--cpu-sample-log2", type=int, default=28)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -316,8 +319,15 @@ def our_arm(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     n = 1 << args.log2n
-    B = args.batch
     pb = not args.no_partial
+    tuned = None
+    if args.tune:
+        # the plain path's autotuner on a 2^min(22, log2n) sample of this workload
+        from gpuheap_gb300 import tune
+        tuned = tune.autotune_sort(log2n=min(22, args.log2n), key=args.key, dist=args.dist, partial_buffer=pb)
+        args.batch, args.variant = tuned["batch_size"], tuned["variant"]
+        args.threads, args.grid, args.owner_depth = tuned["threads"], tuned["grid"], tuned["owner_depth"]
+    B = args.batch
     s = 8 if args.key == "u64" else 4
     tdt = torch.int64 if args.key == "u64" else torch.int32
     bn = 1
@@ -439,7 +449,8 @@ def our_arm(args):
         "metric": METRIC.format(log2n=args.log2n, key=args.key), "value": round(value, 3), "unit": "M keys/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": args.key, "data": "synthetic",
-        "config": dict(workload_config(args), block_threads=info["block_threads"], grid=info["grid"]),
+        "config": dict(workload_config(args), block_threads=info["block_threads"], grid=info["grid"],
+                       **({"tuned": tuned} if tuned else {})),
         "phases_ms": {"reset": round(statistics.mean(t_reset), 3), "insert": round(ti, 3), "delete": round(td, 3)},
         "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
         "owner_delete": owner,
