@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--threads", type=int, default=0, help="threads per block (0: automatic)")
     p.add_argument("--tune", action="store_true",
                    help="heapsort: pick batch size, layout, threads, blocks and owner depth with the autotuner "
-                        "(gpuheap_gb300.tune) on a 2^22 sample first")
+                        "(gpuheap_gb300.tune) on a 2^24 sample first")
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--cpu-sample-log2", type=int, default=28)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -322,9 +322,9 @@ def our_arm(args):
     pb = not args.no_partial
     tuned = None
     if args.tune:
-        # the plain path's autotuner on a 2^min(22, log2n) sample of this workload
+        # the plain path's autotuner on a 2^min(24, log2n) sample of this workload
         from gpuheap_gb300 import tune
-        tuned = tune.autotune_sort(log2n=min(22, args.log2n), key=args.key, dist=args.dist, partial_buffer=pb)
+        tuned = tune.autotune_sort(log2n=min(24, args.log2n), key=args.key, dist=args.dist, partial_buffer=pb)
         args.batch, args.variant = tuned["batch_size"], tuned["variant"]
         args.threads, args.grid, args.owner_depth = tuned["threads"], tuned["grid"], tuned["owner_depth"]
     B = args.batch

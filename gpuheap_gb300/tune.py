@@ -90,7 +90,7 @@ def _cache_path():
     return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune_cache.json")
 
 
-def autotune_sort(log2n=22, key="u32", dist="uniform", partial_buffer=True, seed=7, reps=2, cache=True, log=None,
+def autotune_sort(log2n=24, key="u32", dist="uniform", partial_buffer=True, seed=7, reps=2, cache=True, log=None,
                   **space):
     """Picks batch size, layout, block threads, blocks and owner depth for
     gh_heap_sort on 2^log2n seeded keys of `dist` ("uniform" or "zipf").
