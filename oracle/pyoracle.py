@@ -45,6 +45,8 @@ def lib():
         so.gho_dijkstra_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int, _VP]
         so.gho_astar_grid.restype = ctypes.c_uint32
         so.gho_astar_grid.argtypes = [ctypes.c_int, ctypes.c_int, _VP, _VP, _VP]
+        so.gho_astar_ref8.restype = ctypes.c_uint32
+        so.gho_astar_ref8.argtypes = [ctypes.c_int, ctypes.c_int, _VP]
         so.gho_astar_grid_sg.restype = ctypes.c_uint32
         so.gho_astar_grid_sg.argtypes = [ctypes.c_int, ctypes.c_int, _VP, ctypes.c_int, ctypes.c_int, _VP, _VP]
         so.gho_astar_grid_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, ctypes.c_int, _VP]
@@ -110,6 +112,14 @@ def dijkstra(rowptr, col, w, sources, threads=1):
     lib().gho_dijkstra_many(n, rowptr.ctypes.data, col.ctypes.data, w.ctypes.data, src.ctypes.data, src.size,
                             threads, out.ctypes.data)
     return out
+
+
+def astar_ref8(bitmap_words, width, height):
+    """The reference's 8-connected bitmap A* restated (gho_astar_ref8):
+    bitmap_words is a uint32 array, bit i set = cell i open."""
+    import numpy as np
+    words = np.ascontiguousarray(bitmap_words, np.uint32)
+    return int(lib().gho_astar_ref8(int(width), int(height), words.ctypes.data))
 
 
 def astar_grid(cost, stats=False):

@@ -114,6 +114,56 @@ uint32_t gho_astar_grid_sg(int width, int height, const uint8_t* cost, int start
     return result;
 }
 
+// The reference's own move model (artifacts/astar/seq_astar.hpp:13-78,
+// SeqAstarSearch :85-183), restated to pin the machinery above: a w x h
+// bitmap (bit i of word i/32 set = cell i open), 8 moves in the order
+// (-1,-1) (0,-1) (+1,-1) (-1,0) (+1,0) (-1,+1) (0,+1) (+1,+1) with the
+// costs 3 2 2 2 1 3 1 2, the heuristic x2 - x1 + y2 - y1 to the corner
+// (w-1, h-1) in 32-bit unsigned arithmetic, an entry skipped when its g is
+// above the cell's best, and the search stopped as soon as a move reaches
+// the corner (open or not) -- the cost then recorded there is the result,
+// UINT32_MAX when the corner was never reached.
+uint32_t gho_astar_ref8(int width, int height, const uint32_t* bitmap) {
+    const uint32_t w = static_cast<uint32_t>(width), h = static_cast<uint32_t>(height);
+    const uint64_t cells = static_cast<uint64_t>(w) * h;
+    auto heur = [&](uint32_t i) { return (w - 1) - i % w + (h - 1) - i / w; };
+    auto open_at = [&](uint32_t i) { return i != 0xffffffffu && ((bitmap[i / 32] >> (i % 32)) & 1u) != 0; };
+    auto cell = [&](uint32_t i, int dx, int dy) -> uint32_t {
+        const int x = static_cast<int>(i % w) + dx, y = static_cast<int>(i / w) + dy;
+        if (x < 0 || y < 0 || x >= static_cast<int>(w) || y >= static_cast<int>(h)) return 0xffffffffu;
+        return w * static_cast<uint32_t>(y) + static_cast<uint32_t>(x);
+    };
+    static const int kDx[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
+    static const int kDy[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+    static const uint32_t kCost[8] = {3, 2, 2, 2, 1, 3, 1, 2};
+    std::vector<uint32_t> best(cells, 0xffffffffu);
+    best[0] = 0;
+    std::priority_queue<uint64_t, std::vector<uint64_t>, std::greater<uint64_t>> open;
+    open.push(static_cast<uint64_t>(heur(0)) << 32);
+    const uint32_t corner = static_cast<uint32_t>(cells - 1);
+    bool stop = false;
+    while (!open.empty() && !stop) {
+        const uint64_t item = open.top();
+        open.pop();
+        const uint32_t v = static_cast<uint32_t>(item);
+        const uint32_t g = static_cast<uint32_t>(item >> 32) - heur(v);
+        if (g > best[v]) continue;
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t u = cell(v, kDx[k], kDy[k]);
+            if (u == corner && u != 0xffffffffu) {
+                best[u] = g + kCost[k];
+                stop = true;
+                break;
+            }
+            if (open_at(u) && best[u] > g + kCost[k]) {
+                best[u] = g + kCost[k];
+                open.push((static_cast<uint64_t>(heur(u) + g + kCost[k]) << 32) | u);
+            }
+        }
+    }
+    return best[corner];
+}
+
 uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* expansions, long long* max_open) {
     return gho_astar_grid_sg(width, height, cost, 0, static_cast<int>(static_cast<int64_t>(width) * height - 1),
                              expansions, max_open);

@@ -9,15 +9,17 @@ phase and at the end.  These vectors pin both the oracle restatement (CPU
 tests) and the CUDA path (GPU tests, one thread block, where the heap is
 deterministic).
 
-Three sets: `small` (bgpq_ref_cases.npz, batch 16-64, every key type and
+Four sets: `small` (bgpq_ref_cases.npz, batch 16-64, every key type and
 scenario), `large` (bgpq_ref_cases_large.npz, batch 256-2048, the batch
-sizes of the heap-sort configurations) and `retrieve`
+sizes of the heap-sort configurations), `astar` (astar_ref_cases.npz:
+bitmaps through the reference's sequential A*, artifacts/astar/
+seq_astar.hpp, pinning the oracle's A* machinery) and `retrieve`
 (retrieve_ref_cases.npz: insert / retrieve sequences through the reference's
 retrieving heap, applications/sssp_longfei_new/heap.cuh, pinning the runs
 that `retrieve` returns and the heap each sequence leaves).
 
 Usage (needs the reference tree; not run by the tests):
-    make -C oracle ref REF=<reference tree> && python tests/golden/make_golden.py [small] [large] [retrieve]
+    make -C oracle ref REF=<reference tree> && python tests/golden/make_golden.py [small] [large] [retrieve] [astar]
 """
 import ctypes
 import json
@@ -248,17 +250,45 @@ def _fn_rr(lib, kind, name, res):
     return fn
 
 
+def astar_cases():
+    """40 seeded bitmaps for the reference's sequential A*
+    (artifacts/astar/seq_astar.hpp): sides 1-200, obstacle shares 0-45 %."""
+    for k in range(40):
+        seed = 12000 + k
+        rng = np.random.default_rng(seed)
+        w = int(rng.integers(1, 201)) if k >= 4 else [1, 2, 3, 7][k]
+        h = int(rng.integers(1, 201)) if k >= 4 else [1, 5, 2, 9][k]
+        share = [0.0, 0.1, 0.25, 0.35, 0.45][k % 5]
+        yield w, h, share, seed, rng
+
+
+def run_astar_case(ref, w, h, share, seed, rng):
+    """Bitmap (bit i set = cell i open, the corners open) and the reference's
+    SeqAstarSearch result on it."""
+    open_ = rng.random(w * h) >= share
+    open_[0] = open_[-1] = True
+    words = np.zeros((w * h + 31) // 32 + 1, np.uint32)
+    for i in np.nonzero(open_)[0]:
+        words[i // 32] |= np.uint32(1) << np.uint32(i % 32)
+    fn = ref.ra_seq_astar
+    fn.restype = ctypes.c_uint32
+    fn.argtypes = [VP, ctypes.c_uint32, ctypes.c_uint32]
+    result = fn(VP(words.ctypes.data), h, w)
+    return dict(words=words, result=np.asarray([result], np.uint32)), dict(width=w, height=h, share=share, seed=seed)
+
+
 SETS = {"small": (small_cases, "bgpq_ref_cases.npz"), "large": (large_cases, "bgpq_ref_cases_large.npz"),
-        "retrieve": (retrieve_cases, "retrieve_ref_cases.npz")}
+        "retrieve": (retrieve_cases, "retrieve_ref_cases.npz"), "astar": (astar_cases, "astar_ref_cases.npz")}
 
 
 def main(argv):
     ref = ctypes.CDLL(LIB)
-    for name in (argv or ["small", "large", "retrieve"]):
+    for name in (argv or ["small", "large", "retrieve", "astar"]):
         gen, fname = SETS[name]
         arrays, meta = {}, []
         for case, params in enumerate(gen()):
-            a, m = (run_retrieve_case if name == "retrieve" else run_case)(ref, *params)
+            runner = {"retrieve": run_retrieve_case, "astar": run_astar_case}.get(name, run_case)
+            a, m = runner(ref, *params)
             arrays.update({f"c{case}_{k}": v for k, v in a.items()})
             meta.append(dict(case=case, **m))
         arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)
