@@ -88,6 +88,7 @@ _SIGS = {
     "gh_batch_set_knapsack_order": (_I, [_VP, _I, _I]),
     "gh_batch_knapsack_switches": (_I, [_VP, _VP, _VP]),
     "gh_batch_add_astar": (_I, [_VP, _I, _I, _VP, ctypes.POINTER(_I)]),
+    "gh_batch_add_astar_bitmap": (_I, [_VP, _I, _I, _VP, ctypes.POINTER(_I)]),
     "gh_batch_add_knapsack": (_I, [_VP, _I, _VP, _VP, _LL, ctypes.POINTER(_I)]),
     "gh_batch_build": (_I, [_VP, _VP]),
     "gh_batch_run": (_I, [_VP, _I, _VP]),

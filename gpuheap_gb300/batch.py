@@ -79,6 +79,11 @@ class Batch:
                     g = np.ascontiguousarray(data, np.uint8)
                     _check(lib().gh_batch_add_astar(h, g.shape[1], g.shape[0], g.ctypes.data, None), "add_astar")
                     self.kinds.append(ASTAR)
+                elif kind == "astar8":  # the reference's 8-neighbour bitmap model
+                    g = np.ascontiguousarray(data, np.uint8)
+                    _check(lib().gh_batch_add_astar_bitmap(h, g.shape[1], g.shape[0], g.ctypes.data, None),
+                           "add_astar_bitmap")
+                    self.kinds.append(ASTAR)
                 else:
                     w, p, cap = data
                     w = np.ascontiguousarray(w, np.int32)

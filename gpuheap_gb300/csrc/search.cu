@@ -55,6 +55,7 @@ struct HostInst {
     int greedy = 0;
     int blocks = 1;
     long long work = 0;  // size estimate for the task order
+    int moves = 4;       // A*: 4 (cost grid) or 8 (the reference's bitmap model)
 };
 
 struct gh_batch {
@@ -191,6 +192,24 @@ gh_status gh_batch_add_astar(gh_batch* b, int width, int height, const unsigned 
     h.height = height;
     h.cost.assign(cost_host, cost_host + static_cast<size_t>(width) * height);
     h.work = static_cast<long long>(width) * height;
+    if (id) *id = static_cast<int>(b->host.size());
+    b->host.push_back(std::move(h));
+    if (b->built) free_device(b);
+    return GH_OK;
+}
+
+gh_status gh_batch_add_astar_bitmap(gh_batch* b, int width, int height, const unsigned char* open_host, int* id) {
+    if (!b || !open_host || width < 1 || height < 1 || static_cast<long long>(width) * height > (1LL << 30))
+        return GH_ERR_INVALID;
+    HostInst h;
+    h.kind = GH_SEARCH_ASTAR;
+    h.moves = 8;
+    h.width = width;
+    h.height = height;
+    const size_t cells = static_cast<size_t>(width) * height;
+    h.cost.resize(cells);
+    for (size_t i = 0; i < cells; ++i) h.cost[i] = open_host[i] ? 1 : 0;
+    h.work = static_cast<long long>(cells);
     if (id) *id = static_cast<int>(b->host.size());
     b->host.push_back(std::move(h));
     if (b->built) free_device(b);
@@ -337,6 +356,7 @@ gh_status gh_batch_build(gh_batch* b, void* stream) {
         if (h.kind == GH_SEARCH_ASTAR) {
             d.width = h.width;
             d.height = h.height;
+            d.moves = h.moves;
             d.start = 0;
             d.goal = h.width * h.height - 1;
             d.cost = A + L.cost;

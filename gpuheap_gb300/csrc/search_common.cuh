@@ -67,12 +67,14 @@ struct alignas(16) Inst {
     int mode;                   // structure in use: 0 heap, 1 FIFO
     int switches;               // mode changes so far
     int tokens;                 // served, device loop: work tokens of the query still out
-    int pad;
+    int moves;                  // A*: 0 or 4, cost grid (4 neighbours); 8, the reference's bitmap model
 };
 
-// Shared memory of a search block, ahead of the heap's region.
+// Shared memory of a search block, ahead of the heap's region.  Emitted
+// keys: a full batch is inserted after every round of one key a thread, so
+// B + 8 T holds what a round adds (an A* key has up to eight neighbours).
 struct SearchSmem {
-    static __host__ __device__ size_t emitKeys(int B, int T) { return static_cast<size_t>(B) + 4 * static_cast<size_t>(T); }
+    static __host__ __device__ size_t emitKeys(int B, int T) { return static_cast<size_t>(B) + 8 * static_cast<size_t>(T); }
     static __host__ __device__ size_t bytes(int B, int T) {
         const size_t keys = (static_cast<size_t>(B) + emitKeys(B, T)) * 8;
         const size_t knap = static_cast<size_t>(kMaxKnapItems + 1) * 16 + static_cast<size_t>(kMaxKnapItems) * 8 +

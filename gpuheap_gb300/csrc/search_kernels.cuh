@@ -186,16 +186,21 @@ __device__ inline void seed_instance(Inst* in) {
     }
 }
 
+// Inserts every full batch of the emitted keys and moves the rest (fewer
+// than B) to the front, so that a round starts with fewer than B keys and
+// its emits fit the B + 8 T slots.  The rest comes from behind at least one
+// batch, so the parallel move never overlaps.
 template <typename H>
 __device__ __forceinline__ void flush_full(const H& heap, u64* emit, int* cnt, int B, int heapOff, unsigned long long& inserted) {
     __syncthreads();
     const int c = *cnt;
     if (c >= B) {
-        gh::app::insert_keys(heap, emit, B, heapOff);
-        for (int i = threadIdx.x; i < c - B; i += blockDim.x) emit[i] = emit[B + i];
+        int off = 0;
+        for (; c - off >= B; off += B) gh::app::insert_keys(heap, emit + off, B, heapOff);
+        for (int i = threadIdx.x; i < c - off; i += blockDim.x) emit[i] = emit[off + i];
         __syncthreads();
-        if (threadIdx.x == 0) *cnt = c - B;
-        inserted += B;
+        if (threadIdx.x == 0) *cnt = c - off;
+        inserted += off;
     }
     __syncthreads();
 }
@@ -286,6 +291,7 @@ __device__ bool run_astar(const H& heap, Inst* in, unsigned char* smem, int heap
     int* ctl = reinterpret_cast<int*>(emit + SearchSmem::emitKeys(B, T));
     const int width = in->width, height = in->height;
     const int goal = in->goal;
+    const bool eight = in->moves == 8;
     unsigned* g = in->g;
     const unsigned char* cost = in->cost;
     unsigned* inc = reinterpret_cast<unsigned*>(&in->incumbent);
@@ -313,14 +319,23 @@ __device__ bool run_astar(const H& heap, Inst* in, unsigned char* smem, int heap
                 if (f < best && gv <= __ldcg(g + v)) {  // not pruned, not stale
                     ++expanded;
                     const int x = v % width, y = v / width;
-                    const int nb[4] = {x > 0 ? v - 1 : -1, x + 1 < width ? v + 1 : -1, y > 0 ? v - width : -1,
-                                       y + 1 < height ? v + width : -1};
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int u = nb[k];
-                        if (u < 0) continue;
-                        const unsigned c = cost[u];
-                        if (c == 0) continue;
+                    for (int k = 0; k < 8; ++k) {
+                        // moves 4: left, right, up, down, each costing the cell
+                        // entered; moves 8: the reference's model
+                        // (artifacts/astar/pq_model.cuh:126-190): the eight
+                        // neighbours in its order, open cells only, each
+                        // direction with its fixed cost 3 2 2 2 1 3 1 2
+                        if (k >= 4 && !eight) break;
+                        const int dx = eight ? (k < 3 ? k - 1 : k < 5 ? (k == 3 ? -1 : 1) : k - 6)
+                                             : (k == 0 ? -1 : k == 1 ? 1 : 0);
+                        const int dy = eight ? (k < 3 ? -1 : k < 5 ? 0 : 1) : (k == 2 ? -1 : k == 3 ? 1 : 0);
+                        const int nx = x + dx, ny = y + dy;
+                        if (nx < 0 || ny < 0 || nx >= width || ny >= height) continue;
+                        const int u = ny * width + nx;
+                        const unsigned cu = cost[u];
+                        if (cu == 0) continue;
+                        const unsigned c = eight ? (0x21312223u >> (4 * k)) & 15u : cu;
                         const unsigned ng = gv + c;
                         if (u == goal) {
                             if (ng < __ldcg(g + u)) atomicMin(g + u, ng);

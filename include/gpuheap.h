@@ -348,6 +348,13 @@ gh_status gh_batch_knapsack_switches(gh_batch* b, int* switches_host, void* stre
  * goal free the same way).  Result: the optimal path cost, UINT32_MAX if the
  * goal is unreachable.  *id (may be NULL) gets the instance index. */
 gh_status gh_batch_add_astar(gh_batch* b, int width, int height, const unsigned char* cost_host, int* id);
+/* Grid A* on the reference's own model (artifacts/astar/pq_model.cuh:
+ * 126-190, astar_map.cuh): open_host[y * width + x] != 0 marks an open
+ * cell, the eight neighbours (-1,-1) (0,-1) (+1,-1) (-1,0) (+1,0) (-1,+1)
+ * (0,+1) (+1,+1) cost 3 2 2 2 1 3 1 2, from (0, 0) to (width-1, height-1)
+ * with the Manhattan heuristic.  Result: the optimal path cost (the
+ * reference's final dist[target]), UINT32_MAX if unreachable. */
+gh_status gh_batch_add_astar_bitmap(gh_batch* b, int width, int height, const unsigned char* open_host, int* id);
 /* 0/1 knapsack with n <= 1024 items (weights >= 1, profits >= 0, total
  * profit < 2^30): best-first branch-and-bound on the Dantzig bound
  * (artifacts/knapsack/knapsackKernel.cuh:4-91).  Result: the optimum. */

@@ -95,6 +95,8 @@ void gho_dijkstra_many(int n, const int64_t* rowptr, const int32_t* col, const u
 uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* expansions, long long* max_open);
 /* The reference's 8-connected bitmap A* (artifacts/astar/seq_astar.hpp:85-183) restated. */
 uint32_t gho_astar_ref8(int width, int height, const uint32_t* bitmap);
+/* The reference's map model searched to the optimum (its GPU A*'s result). */
+uint32_t gho_astar_grid8(int width, int height, const uint8_t* open_cells, long long* expansions);
 /* The same between any start and goal cell (y * width + x). */
 uint32_t gho_astar_grid_sg(int width, int height, const uint8_t* cost, int start, int goal, long long* expansions,
                            long long* max_open);

@@ -45,6 +45,8 @@ def lib():
         so.gho_dijkstra_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int, _VP]
         so.gho_astar_grid.restype = ctypes.c_uint32
         so.gho_astar_grid.argtypes = [ctypes.c_int, ctypes.c_int, _VP, _VP, _VP]
+        so.gho_astar_grid8.restype = ctypes.c_uint32
+        so.gho_astar_grid8.argtypes = [ctypes.c_int, ctypes.c_int, _VP, _VP]
         so.gho_astar_ref8.restype = ctypes.c_uint32
         so.gho_astar_ref8.argtypes = [ctypes.c_int, ctypes.c_int, _VP]
         so.gho_astar_grid_sg.restype = ctypes.c_uint32
@@ -120,6 +122,15 @@ def astar_ref8(bitmap_words, width, height):
     import numpy as np
     words = np.ascontiguousarray(bitmap_words, np.uint32)
     return int(lib().gho_astar_ref8(int(width), int(height), words.ctypes.data))
+
+
+def astar_grid8(open_cells):
+    """Optimal cost from (0, 0) to the last cell on the reference's map
+    model (gho_astar_grid8): open_cells (h, w) nonzero = open, eight moves
+    costing 3 2 2 2 1 3 1 2; UINT32_MAX if unreachable."""
+    import numpy as np
+    g = np.ascontiguousarray(open_cells, np.uint8)
+    return int(lib().gho_astar_grid8(g.shape[1], g.shape[0], g.ctypes.data, None))
 
 
 def astar_grid(cost, stats=False):

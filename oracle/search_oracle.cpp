@@ -164,6 +164,51 @@ uint32_t gho_astar_ref8(int width, int height, const uint32_t* bitmap) {
     return best[corner];
 }
 
+// The reference's map model searched to the optimum (the result of its GPU
+// A*, artifacts/astar/pq_model.cuh, which prunes on dist[target] until no
+// key below it is left): open[i] != 0 marks an open cell, the eight moves
+// and costs of gho_astar_ref8, the Manhattan heuristic (consistent: a
+// straight move costs at least 1, a diagonal one at least 2), the goal
+// (w-1, h-1) taken when popped.
+uint32_t gho_astar_grid8(int width, int height, const uint8_t* open_cells, long long* expansions) {
+    const int64_t cells = static_cast<int64_t>(width) * height;
+    const int goal = static_cast<int>(cells - 1);
+    auto heur = [&](int v) { return static_cast<uint32_t>((width - 1 - v % width) + (height - 1 - v / width)); };
+    static const int kDx[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
+    static const int kDy[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+    static const uint32_t kCost[8] = {3, 2, 2, 2, 1, 3, 1, 2};
+    std::vector<uint32_t> g(cells, 0xffffffffu);
+    std::priority_queue<uint64_t, std::vector<uint64_t>, std::greater<uint64_t>> open;
+    long long exp = 0;
+    uint32_t result = 0xffffffffu;
+    if (open_cells[0] != 0 && open_cells[goal] != 0) {
+        g[0] = 0;
+        open.push(static_cast<uint64_t>(heur(0)) << 32);
+    }
+    while (!open.empty()) {
+        const uint64_t key = open.top();
+        open.pop();
+        const int v = static_cast<int>(key & 0xffffffffu);
+        if (static_cast<uint32_t>(key >> 32) != g[v] + heur(v)) continue;  // stale entry
+        if (v == goal) { result = g[v]; break; }
+        ++exp;
+        const int x = v % width, y = v / width;
+        for (int k = 0; k < 8; ++k) {
+            const int nx = x + kDx[k], ny = y + kDy[k];
+            if (nx < 0 || ny < 0 || nx >= width || ny >= height) continue;
+            const int u = ny * width + nx;
+            if (open_cells[u] == 0) continue;
+            const uint32_t ng = g[v] + kCost[k];
+            if (ng < g[u]) {
+                g[u] = ng;
+                open.push((static_cast<uint64_t>(ng + heur(u)) << 32) | static_cast<uint32_t>(u));
+            }
+        }
+    }
+    if (expansions) *expansions = exp;
+    return result;
+}
+
 uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* expansions, long long* max_open) {
     return gho_astar_grid_sg(width, height, cost, 0, static_cast<int>(static_cast<int64_t>(width) * height - 1),
                              expansions, max_open);

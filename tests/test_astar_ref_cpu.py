@@ -47,3 +47,31 @@ def test_reference_host_run_reproduces_the_vectors(i):
     m = META[i]
     words = np.ascontiguousarray(DATA[f"c{i}_words"], np.uint32)
     assert fn(ctypes.c_void_p(words.ctypes.data), m["height"], m["width"]) == int(DATA[f"c{i}_result"][0])
+
+
+def test_optimal_eight_neighbour_oracle_equals_dijkstra():
+    """gho_astar_grid8 (the reference's map model searched to the optimum,
+    the result of its GPU A*) against scipy's Dijkstra on the same graph."""
+    sp = pytest.importorskip("scipy.sparse")
+    cg = pytest.importorskip("scipy.sparse.csgraph")
+    dx, dy, cost = [-1, 0, 1, -1, 1, -1, 0, 1], [-1, -1, -1, 0, 0, 1, 1, 1], [3, 2, 2, 2, 1, 3, 1, 2]
+    rng = np.random.default_rng(5)
+    for _ in range(120):
+        w, h = int(rng.integers(1, 25)), int(rng.integers(1, 25))
+        o = (rng.random((h, w)) >= rng.choice([0.0, 0.2, 0.4])).astype(np.uint8)
+        o[0, 0] = o[-1, -1] = 1
+        rows, cols, vals = [], [], []
+        for y in range(h):
+            for x in range(w):
+                if not o[y, x]:
+                    continue
+                for k in range(8):
+                    nx, ny = x + dx[k], y + dy[k]
+                    if 0 <= nx < w and 0 <= ny < h and o[ny, nx]:
+                        rows.append(y * w + x)
+                        cols.append(ny * w + nx)
+                        vals.append(cost[k])
+        g = sp.csr_matrix((vals, (rows, cols)), shape=(w * h, w * h))
+        d = cg.dijkstra(g, indices=0)[-1]
+        want = 0xFFFFFFFF if np.isinf(d) else int(d)
+        assert pyoracle.astar_grid8(o) == want

@@ -173,3 +173,49 @@ def test_batch_rejects_bad_arguments():
         gb.Batch([("astar", gb.gen_grid(8, 1))], batch_size=100)
     with pytest.raises(Exception):
         gb.Batch([("knapsack", (np.ones(2000, np.int32), np.ones(2000, np.int32), 5))])
+
+
+@pytest.mark.parametrize("bs,variant", [(64, "bottomup"), (256, "topdown"), (512, "bottomup")])
+def test_astar_on_the_reference_map_model(bs, variant):
+    """A* instances on the reference's own model (eight neighbours with its
+    direction costs over an open/blocked bitmap, gh_batch_add_astar_bitmap)
+    next to cost-grid A* and knapsack instances: every result equals the
+    optimum of the matching oracle, in every mode."""
+    rng = np.random.default_rng(33)
+    inst = []
+    inst.append(("astar8", np.ones((1, 1), np.uint8)))
+    inst.append(("astar8", np.ones((1, 40), np.uint8)))
+    walled = np.ones((30, 30), np.uint8)
+    walled[:, 15] = 0
+    inst.append(("astar8", walled))  # the diagonal moves cannot cross a full wall either
+    gap = walled.copy()
+    gap[29, 15] = 1
+    inst.append(("astar8", gap))
+    for i in range(16):
+        w, h = int(rng.integers(8, 400)), int(rng.integers(8, 400))
+        o = (rng.random((h, w)) >= [0.0, 0.2, 0.35, 0.45][i % 4]).astype(np.uint8)
+        o[0, 0] = o[-1, -1] = 1
+        inst.append(("astar8", o))
+    for i in range(6):
+        side = int(rng.integers(8, 200))
+        inst.append(("astar", gb.gen_grid(side, 300 + i)))
+        inst.append(("knapsack", gb.gen_knapsack(int(rng.integers(2, 200)), 400 + i)))
+    want = []
+    for kind, d in inst:
+        if kind == "astar8":
+            want.append(pyoracle.astar_grid8(d))
+        elif kind == "astar":
+            want.append(int(pyoracle.astar_grid_many([d], threads=1)[0]))
+        else:
+            want.append(int(pyoracle.knap_bb_many([d], threads=1)[0]))
+    want = np.array(want, np.int64)
+    assert want[2] == 0xFFFFFFFF and want[3] != 0xFFFFFFFF
+    b = gb.Batch(inst, batch_size=bs, variant=variant, astar_cells_per_block=1 << 12)
+    try:
+        for mode in ("persistent", "graph", "plain"):
+            b.run(mode)
+            res, st, _ = b.results()
+            assert not st.any()
+            assert np.array_equal(res, want), (mode, np.nonzero(res != want))
+    finally:
+        b.close()
