@@ -51,6 +51,7 @@ _SIGS = {
     "gh_heap_delete_batch": (_I, [_VP, _VP, ctypes.POINTER(_I), _VP]),
     "gh_heap_retrieve": (_I, [_VP, _VP, _I, ctypes.POINTER(_I), _VP]),
     "gh_heap_sort": (_I, [_VP, _VP, _LL, _VP, _VP]),
+    "gh_heap_sort_host": (_I, [_VP, _VP, _LL, _VP, _VP]),
     "gh_heap_check": (_I, [_VP, ctypes.POINTER(_I), ctypes.c_char_p, _I, _VP]),
     "gh_heap_item_count": (_I, [_VP, ctypes.POINTER(_LL)]),
     "gh_heap_node_count": (_I, [_VP, ctypes.POINTER(_I)]),
@@ -367,6 +368,18 @@ class Heap:
         """Heap-sort: reset, insert all keys, delete all (test/partial_heap_test.cu:88-176)."""
         n = keys.numel() if n is None else int(n)
         _check(lib().gh_heap_sort(self._h, _ptr(keys), n, _ptr(out), _stream(stream)), "sort")
+
+    def sort_host(self, keys, out, n=None, stream=None):
+        """Heap-sort with host buffers (gh_heap_sort_host): keys and out are
+        CPU tensors (pinned for overlap) or numpy arrays; the copies overlap
+        the inserts and deletes.  Queued on `stream`; sync() waits."""
+        if hasattr(keys, "data_ptr"):
+            kp, op = keys.data_ptr(), out.data_ptr()
+            n = keys.numel() if n is None else int(n)
+        else:
+            kp, op = keys.ctypes.data, out.ctypes.data
+            n = keys.size if n is None else int(n)
+        _check(lib().gh_heap_sort_host(self._h, kp, n, op, _stream(stream)), "sort_host")
 
     def sync(self, stream=None):
         _check(lib().gh_heap_sync(self._h, _stream(stream)), "sync")

@@ -30,6 +30,12 @@ struct gh_heap {
     gh::impl::CheckResult* check;  // device scratch for gh_heap_check
     int* opSize;                   // device word for gh_heap_delete_batch
     void* scratch;                 // one batch of keys for gh_heap_retrieve
+    // gh_heap_sort_host: device staging buffers, a copy stream and its events
+    void* stageIn = nullptr;
+    void* stageOut = nullptr;
+    size_t stageBytes = 0;
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t sortEv[2 * 8 + 2] = {};
 };
 
 namespace {
@@ -206,6 +212,11 @@ gh_status gh_heap_destroy(gh_heap* h) {
     if (h->opSize) cudaFree(h->opSize);
     if (h->scratch) cudaFree(h->scratch);
     if (h->d.mbox) cudaFree(h->d.mbox);
+    if (h->stageIn) cudaFree(h->stageIn);
+    if (h->stageOut) cudaFree(h->stageOut);
+    for (cudaEvent_t e : h->sortEv)
+        if (e) cudaEventDestroy(e);
+    if (h->copyStream) cudaStreamDestroy(h->copyStream);
     delete h;
     return GH_OK;
 }
@@ -462,6 +473,69 @@ gh_status gh_heap_sort(gh_heap* h, const void* in_dev, long long n, void* out_de
     st = gh_heap_delete(h, out_dev, n, &got, stream);
     if (st != GH_OK) return st;
     return got == n ? GH_OK : GH_ERR_STATE;
+}
+
+gh_status gh_heap_sort_host(gh_heap* h, const void* keys_host, long long n, void* out_host, void* stream) {
+    gh::trace::Range range_("gh_heap_sort_host");
+    constexpr int kPieces = 8;
+    if (!h || n < 0 || (n > 0 && (!keys_host || !out_host))) return GH_ERR_INVALID;
+    if (n > static_cast<long long>(h->d.batchNum) * h->d.batchSize) return GH_ERR_CAPACITY;
+    const int B = h->d.batchSize;
+    if (!h->d.pb && n % B != 0) return GH_ERR_INVALID;  // a padded last batch would not fit the output
+    if (n == 0) return GH_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t kb = static_cast<size_t>(h->d.keyBytes), bytes = static_cast<size_t>(n) * kb;
+    if (h->stageBytes < bytes) {
+        if (h->stageIn) cudaFree(h->stageIn);
+        if (h->stageOut) cudaFree(h->stageOut);
+        h->stageIn = h->stageOut = nullptr;
+        h->stageBytes = 0;
+        GH_CUDA(cudaMalloc(&h->stageIn, bytes));
+        GH_CUDA(cudaMalloc(&h->stageOut, bytes));
+        h->stageBytes = bytes;
+    }
+    if (!h->copyStream) {
+        GH_CUDA(cudaStreamCreateWithFlags(&h->copyStream, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : h->sortEv) GH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    cudaStream_t c = h->copyStream;
+    unsigned char* in = static_cast<unsigned char*>(h->stageIn);
+    unsigned char* out = static_cast<unsigned char*>(h->stageOut);
+    const unsigned char* hin = static_cast<const unsigned char*>(keys_host);
+    unsigned char* hout = static_cast<unsigned char*>(out_host);
+    // pieces of whole batches: the bulk insert reserves full batches, and the
+    // deletes of a piece end on a batch boundary
+    const long long per = (n + kPieces - 1) / kPieces;
+    const long long piece = std::max<long long>(B, (per + B - 1) / B * B);
+    int e = 0;
+    // the copies start once the caller's stream is done with the staging buffers
+    GH_CUDA(cudaEventRecord(h->sortEv[e], s));
+    GH_CUDA(cudaStreamWaitEvent(c, h->sortEv[e++], 0));
+    gh_status st = fill_items(h, s);
+    if (st != GH_OK) return st;
+    // keys in: piece i crosses on the copy stream while piece i - 1 is inserted
+    for (long long off = 0; off < n; off += piece) {
+        const long long len = std::min(piece, n - off);
+        GH_CUDA(cudaMemcpyAsync(in + off * kb, hin + off * kb, len * kb, cudaMemcpyHostToDevice, c));
+        GH_CUDA(cudaEventRecord(h->sortEv[e], c));
+        GH_CUDA(cudaStreamWaitEvent(s, h->sortEv[e++], 0));
+        st = gh_heap_insert(h, in + off * kb, len, B, stream);
+        if (st != GH_OK) return st;
+    }
+    // keys out: piece j is deleted on the caller's stream, then crosses on
+    // the copy stream while piece j + 1 is deleted
+    for (long long off = 0; off < n; off += piece) {
+        const long long len = std::min(piece, n - off);
+        st = delete_bulk(h, out + off * kb, len, nullptr, nullptr, stream);
+        if (st != GH_OK) return st;
+        GH_CUDA(cudaEventRecord(h->sortEv[e], s));
+        GH_CUDA(cudaStreamWaitEvent(c, h->sortEv[e++], 0));
+        GH_CUDA(cudaMemcpyAsync(hout + off * kb, out + off * kb, len * kb, cudaMemcpyDeviceToHost, c));
+    }
+    // the caller's stream ends after the last copy
+    GH_CUDA(cudaEventRecord(h->sortEv[e], c));
+    GH_CUDA(cudaStreamWaitEvent(s, h->sortEv[e], 0));
+    return GH_OK;
 }
 
 gh_status gh_heap_check(gh_heap* h, int* ok, char* msg, int msg_len, void* stream) {

@@ -143,6 +143,16 @@ gh_status gh_heap_retrieve(gh_heap* h, void* out_dev, int size, int* n_out, void
  * delete everything into out_dev[0, n).  out_dev must hold n keys. */
 gh_status gh_heap_sort(gh_heap* h, const void* in_dev, long long n, void* out_dev, void* stream);
 
+/* The heap-sort with host buffers: keys_host[0, n) in, out_host[0, n) in key
+ * order.  The copies cross on a stream of the heap's own in eight pieces of
+ * whole batches: piece i goes in while piece i - 1 is inserted, and piece j
+ * comes out while piece j + 1 is deleted, so the host link hides behind the
+ * inserts and deletes (pinned host memory lets the copies overlap; pageable
+ * memory works without the overlap).  Device staging buffers of n keys each
+ * stay with the heap for the next call.  `stream` ends after the last copy.
+ * Heaps without the partial buffer need n to be a multiple of batch_size. */
+gh_status gh_heap_sort_host(gh_heap* h, const void* keys_host, long long n, void* out_host, void* stream);
+
 /* checkInsertHeap(): heap/tditdd/heap.cuh:123-176, heap/buitdd/heap.cuh:118-172,
  * run on the device over the whole heap.  *ok = 1 when valid; otherwise msg
  * (if not NULL) describes the first violation.  Synchronizes the stream. */

@@ -62,6 +62,7 @@ def test_rejects_bad_arguments_before_touching_a_device(ghlib):
     assert ghlib.gh_serve_destroy(None) == 1
     assert ghlib.gh_serve_step(None, None, None, None, None) == 1
     assert ghlib.gh_serve_submit(None, 2, 0, 0, 0, None) == 1
+    assert ghlib.gh_heap_sort_host(None, None, 0, None, None) == 1
     assert ghlib.gh_rheap_create(None, 2, 64, 64, None) == 1
     assert ghlib.gh_rheap_destroy(None) == 1
     assert ghlib.gh_rheap_insert(None, None, 1, None) == 1

@@ -526,3 +526,33 @@ def test_device_key_generator_matches_oracle(key, dist):
     n = (1 << 18) + 17
     got = to_host(gh.gen_keys(key, 1234, dist, n), key)
     assert np.array_equal(got, pyoracle.gen(key, 1234, dist, n))
+
+
+@pytest.mark.parametrize("key,B,pb,n", [("u32", 2048, True, (1 << 22) + 777), ("u64", 1024, True, (1 << 20) + 5),
+                                       ("i32", 512, False, 3000 * 512), ("u32", 256, True, 100)])
+def test_sort_host_buffers(key, B, pb, n):
+    """gh_heap_sort_host: pinned host keys in, host output in key order, the
+    copies overlapped in pieces; repeated and with a larger n (the staging
+    buffers grow); pageable numpy buffers work too."""
+    dt = {"u32": torch.int32, "i32": torch.int32, "u64": torch.int64}[key]
+    bn = 1
+    while bn * B < 4 * n:
+        bn <<= 1
+    with gh.Heap(bn, B, key=key, partial_buffer=pb) as h:
+        for m in (n // 2 // B * B or n, n):
+            keys = gh.gen_keys(key, 31 + m, "uniform", m)
+            want = gh.sort_keys(keys, key).cpu()
+            hin = keys.cpu().pin_memory()
+            hout = torch.empty(m, dtype=dt).pin_memory()
+            h.sort_host(hin, hout)
+            h.sync()
+            assert torch.equal(hout, want)
+        npin = keys.cpu().numpy().copy()
+        npout = np.zeros_like(npin)
+        h.sort_host(npin, npout)
+        h.sync()
+        assert np.array_equal(npout, want.numpy())
+    if not pb:
+        with gh.Heap(bn, B, key=key, partial_buffer=False) as h:
+            with pytest.raises(Exception):
+                h.sort_host(np.zeros(B + 1, np.int32), np.zeros(B + 1, np.int32))
