@@ -43,6 +43,22 @@ inline cudaError_t allow_smem(const void* fn, size_t smem) {
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
 }
 
+// At most as many blocks as the GPU holds at once.  The reserved bulk insert
+// hands batch j to block j mod grid, and an insert may wait for a parent
+// target that an earlier batch fills; the owner-mode delete's owner waits
+// for workers.  Both make progress only if every block runs, so a grid
+// larger than the resident set would wait until the time limit.
+inline int resident_grid(const void* fn, int threads, size_t smem, int want) {
+    int per = 0, dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, smem) != cudaSuccess || per < 1) {
+        cudaGetLastError();
+        return want;
+    }
+    const long long cap = static_cast<long long>(per) * sms;
+    return want < cap ? want : static_cast<int>(cap);
+}
+
 // Calls f(Heap<K, V, PB, IPT>{}) for the run-time variant, pb flag and IPT.
 template <typename K, typename F>
 inline cudaError_t dispatch(const Desc& d, int threads, F&& f) {
@@ -100,7 +116,9 @@ cudaError_t launch_insert(const LaunchArgs& a, const K* keys, long long n, int c
             const long long mb = (m + 255) / 256;
             k_mark_reserved<<<static_cast<int>(mb < 1024 ? mb : 1024), 256, 0, a.stream>>>(a.d->state, a.d->status, held);
             count_launch();
-            k_insert_reserved<H, K><<<static_cast<int>(m < a.grid ? m : a.grid), a.threads, smem, a.stream>>>(h, keys, m);
+            const int g = resident_grid(reinterpret_cast<const void*>(k_insert_reserved<H, K>), a.threads, smem,
+                                        static_cast<int>(m < a.grid ? m : a.grid));
+            k_insert_reserved<H, K><<<g, a.threads, smem, a.stream>>>(h, keys, m);
             count_launch();
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
@@ -149,7 +167,8 @@ cudaError_t launch_erase(const LaunchArgs& a, K* out, const K* threshold) {
             if (e2 != cudaSuccess) return e2;
             Mailbox* mb = static_cast<Mailbox*>(a.d->mbox);
             K* mdata = reinterpret_cast<K*>(static_cast<char*>(a.d->mbox) + sizeof(Mailbox));
-            k_delete_owner<H, K><<<a.grid, 1024, smem, a.stream>>>(h, out, mb, mdata, R);
+            const int g = resident_grid(reinterpret_cast<const void*>(k_delete_owner<H, K>), 1024, smem, a.grid);
+            k_delete_owner<H, K><<<g, 1024, smem, a.stream>>>(h, out, mb, mdata, R);
             count_launch();
             return cudaGetLastError();
         });

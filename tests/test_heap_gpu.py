@@ -556,3 +556,19 @@ def test_sort_host_buffers(key, B, pb, n):
         with gh.Heap(bn, B, key=key, partial_buffer=False) as h:
             with pytest.raises(Exception):
                 h.sort_host(np.zeros(B + 1, np.int32), np.zeros(B + 1, np.int32))
+
+
+@pytest.mark.parametrize("variant", ["bottomup", "topdown"])
+def test_sort_with_more_blocks_than_the_gpu_holds(variant):
+    """A grid of three blocks per SM: the reserved bulk insert and the
+    owner-mode delete run at most the resident blocks (their blocks wait on
+    each other), the result is exact and no wait runs out."""
+    B, n = 2048, 1 << 22
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    keys = gh.gen_keys("u32", 71, "uniform", n)
+    out = torch.empty_like(keys)
+    with gh.Heap(4 * n // B, B, key="u32", variant=variant) as h:
+        h.set_grid(3 * sms)
+        h.sort(keys, out)
+        h.sync()
+        assert torch.equal(out, gh.sort_keys(keys, "u32"))
