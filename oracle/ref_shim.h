@@ -81,7 +81,22 @@ inline unsigned atomicCAS(unsigned* a, unsigned cmp, unsigned val) {
 
 typedef int cudaError_t;
 enum ShimMemcpyKind { cudaMemcpyHostToDevice = 1, cudaMemcpyDeviceToHost = 2, cudaMemcpyDeviceToDevice = 3 };
-inline cudaError_t cudaMalloc(void** p, size_t n) { *p = std::calloc(n ? n : 1, 1); return *p ? 0 : 2; }
+// Device allocations come back zeroed, with as much room again behind them
+// filled with 0x7f bytes.  On a padded node the reference's top-down sift
+// without the partial buffer reads lock words past its status array
+// (tditdd_np/heap.cuh:356, found with AddressSanitizer).  In that room they
+// read 0x7f7f7f7f, neither AVAIL nor INUSE, which the sift takes as "no
+// valid child" (:352-354).  The outcome is then the same on every run,
+// instead of depending on whatever the host heap held there.
+inline cudaError_t cudaMalloc(void** p, size_t n) {
+    const size_t m = n ? n : 1;
+    unsigned char* q = static_cast<unsigned char*>(std::malloc(2 * m + 4096));
+    if (!q) return 2;
+    std::memset(q, 0, m);
+    std::memset(q + m, 0x7f, m + 4096);
+    *p = q;
+    return 0;
+}
 inline cudaError_t cudaFree(void* p) { std::free(p); return 0; }
 inline cudaError_t cudaMemcpy(void* d, const void* s, size_t n, int) { std::memmove(d, s, n); return 0; }
 inline cudaError_t cudaMemset(void* p, int v, size_t n) { std::memset(p, v, n); return 0; }

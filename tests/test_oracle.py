@@ -231,9 +231,13 @@ def test_reference_loses_padded_keys():
     tie) loses the real keys of a padded node in the sequence below; the
     model keeps them.  The host run is deterministic: every call of the
     reference starts from a cleared shared-memory stand-in and spin counter
-    (oracle/ref_driver.cpp), so it runs to the end and the same keys are
-    lost whatever ran before it.  Runs only where oracle/_ref holds the
-    reference's heaps compiled for the host (built from the reference tree)."""
+    (oracle/ref_driver.cpp), and on this sequence its sift reads lock words
+    past the end of its status array (tditdd_np/heap.cuh:356), which land in
+    the room the shim's allocations keep behind them, filled with a value it
+    takes as "no child" (oracle/ref_shim.h).  Before that room existed those
+    reads saw whatever the host heap held, and about one full test run in six
+    stopped here.  Runs only where oracle/_ref holds the reference's heaps
+    compiled for the host (built from the reference tree)."""
     import ctypes
     import os
     lib_path = os.path.join(os.path.dirname(pyoracle.HERE), "oracle", "_ref", "libbgpq_ref.so")
