@@ -103,6 +103,7 @@ _SIGS = {
     "gh_serve_set_blocks": (_I, [_VP, _LL, _I, _LL, _I]),
     "gh_serve_add_graph": (_I, [_VP, _I, _VP, _VP, _VP, ctypes.POINTER(_I)]),
     "gh_serve_add_map": (_I, [_VP, _I, _I, _VP, ctypes.POINTER(_I)]),
+    "gh_serve_add_bitmap": (_I, [_VP, _I, _I, _VP, ctypes.POINTER(_I)]),
     "gh_serve_submit": (_I, [_VP, _I, _I, _I, _I, ctypes.POINTER(_LL)]),
     "gh_serve_step": (_I, [_VP, _VP, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "gh_serve_result": (_I, [_VP, _LL, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_ulonglong),

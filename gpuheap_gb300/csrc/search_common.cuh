@@ -133,8 +133,10 @@ struct alignas(16) ServeReq {
     const int* col;
     const unsigned* w;
     const unsigned char* cost;
+    int moves;  // A*: 4 (cost grid) or 8 (the reference's bitmap model)
+    int pad[3];
 };
-static_assert(sizeof(ServeReq) == 96, "request record layout");
+static_assert(sizeof(ServeReq) == 112, "request record layout");
 
 // A completion (the device writes every field, then seq).
 struct alignas(16) ServeDone {

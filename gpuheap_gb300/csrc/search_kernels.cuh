@@ -717,7 +717,7 @@ __device__ inline void unlock(ServeDev* d) {
     atomicExch(&d->lock, 0);
 }
 
-// 96-byte request records, word by word.
+// Request records, word by word.
 __device__ inline void copy_req(volatile ServeReq* dst, const volatile ServeReq* src) {
     volatile u64* o = reinterpret_cast<volatile u64*>(dst);
     const volatile u64* i = reinterpret_cast<const volatile u64*>(src);
@@ -911,6 +911,7 @@ __device__ inline void setup_query(ServeDev* d, int slot, int B) {
             in->width = q->width;
             in->height = q->height;
             in->cost = q->cost;
+            in->moves = q->moves;
             in->start = q->a;
             in->goal = q->b;
         }

@@ -50,6 +50,7 @@ struct Dataset {
     const int* col = nullptr;
     const unsigned* w = nullptr;
     const unsigned char* cost = nullptr;
+    int moves = 4;  // A* maps: 4 (cost grid) or 8 (the reference's bitmap model)
 };
 
 struct Query {
@@ -192,6 +193,7 @@ Inst make_inst(gh_server* s, const Query& q) {
         in.width = d.width;
         in.height = d.height;
         in.cost = d.cost;
+        in.moves = d.moves;
         in.start = q.a;
         in.goal = q.b;
     }
@@ -232,6 +234,7 @@ void post_requests(gh_server* s) {
         r->col = d.col;
         r->w = d.w;
         r->cost = d.cost;
+        r->moves = d.moves;
         __atomic_store_n(&r->seq, s->posted + 1, __ATOMIC_RELEASE);
         ++s->posted;
         q.state = 1;
@@ -454,6 +457,12 @@ gh_status gh_serve_add_map(gh_server* s, int width, int height, const unsigned c
     if (id) *id = static_cast<int>(s->data.size());
     s->data.push_back(d);
     return GH_OK;
+}
+
+gh_status gh_serve_add_bitmap(gh_server* s, int width, int height, const unsigned char* open_dev, int* id) {
+    const gh_status st = gh_serve_add_map(s, width, height, open_dev, id);
+    if (st == GH_OK) s->data.back().moves = 8;
+    return st;
 }
 
 gh_status gh_serve_submit(gh_server* s, int kind, int dataset, int a, int b, long long* query) {

@@ -52,6 +52,15 @@ class Server:
         self._keep.append(cost)
         return i.value
 
+    def add_bitmap(self, open_cells):
+        """A resident (height, width) uint8 map on the reference's model
+        (nonzero = open, eight moves with its direction costs); returns its id."""
+        i = _I()
+        h, w = open_cells.shape
+        _check(lib().gh_serve_add_bitmap(self._h, w, h, open_cells.data_ptr(), ctypes.byref(i)), "serve_add_bitmap")
+        self._keep.append(open_cells)
+        return i.value
+
     def submit(self, kind, dataset, a, b=0):
         """Queues SSSP (kind SSSP, from vertex a) or A* (kind ASTAR, cell a to cell b); returns the query id."""
         q = _LL()

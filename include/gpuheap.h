@@ -429,6 +429,10 @@ gh_status gh_serve_set_blocks(gh_server* s, long long vertices_per_block, int ss
 gh_status gh_serve_add_graph(gh_server* s, int n, const long long* rowptr_dev, const int* col_dev,
                              const unsigned* w_dev, int* id);
 gh_status gh_serve_add_map(gh_server* s, int width, int height, const unsigned char* cost_dev, int* id);
+/* A map on the reference's own model, as in gh_batch_add_astar_bitmap:
+ * open_dev[y * width + x] != 0 marks an open cell; eight moves with the
+ * reference's direction costs.  A* queries on it go from cell a to cell b. */
+gh_status gh_serve_add_bitmap(gh_server* s, int width, int height, const unsigned char* open_dev, int* id);
 /* Queues a query: GH_SEARCH_SSSP on graph `dataset` from vertex a (b unused),
  * or GH_SEARCH_ASTAR on map `dataset` from cell a to cell b.  *query gets its
  * id.  GH_ERR_CAPACITY if the query could never fit the arena. */

@@ -97,6 +97,8 @@ uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* e
 uint32_t gho_astar_ref8(int width, int height, const uint32_t* bitmap);
 /* The reference's map model searched to the optimum (its GPU A*'s result). */
 uint32_t gho_astar_grid8(int width, int height, const uint8_t* open_cells, long long* expansions);
+uint32_t gho_astar_grid8_sg(int width, int height, const uint8_t* open_cells, int start, int goal,
+                            long long* expansions);
 /* The same between any start and goal cell (y * width + x). */
 uint32_t gho_astar_grid_sg(int width, int height, const uint8_t* cost, int start, int goal, long long* expansions,
                            long long* max_open);

@@ -45,6 +45,8 @@ def lib():
         so.gho_dijkstra_many.argtypes = [ctypes.c_int, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int, _VP]
         so.gho_astar_grid.restype = ctypes.c_uint32
         so.gho_astar_grid.argtypes = [ctypes.c_int, ctypes.c_int, _VP, _VP, _VP]
+        so.gho_astar_grid8_sg.restype = ctypes.c_uint32
+        so.gho_astar_grid8_sg.argtypes = [ctypes.c_int, ctypes.c_int, _VP, ctypes.c_int, ctypes.c_int, _VP]
         so.gho_astar_grid8.restype = ctypes.c_uint32
         so.gho_astar_grid8.argtypes = [ctypes.c_int, ctypes.c_int, _VP, _VP]
         so.gho_astar_ref8.restype = ctypes.c_uint32
@@ -131,6 +133,13 @@ def astar_grid8(open_cells):
     import numpy as np
     g = np.ascontiguousarray(open_cells, np.uint8)
     return int(lib().gho_astar_grid8(g.shape[1], g.shape[0], g.ctypes.data, None))
+
+
+def astar_grid8_sg(open_cells, start, goal):
+    """As astar_grid8, from cell `start` to cell `goal` (Manhattan heuristic to the goal)."""
+    import numpy as np
+    g = np.ascontiguousarray(open_cells, np.uint8)
+    return int(lib().gho_astar_grid8_sg(g.shape[1], g.shape[0], g.ctypes.data, int(start), int(goal), None))
 
 
 def astar_grid(cost, stats=False):

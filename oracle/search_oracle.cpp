@@ -170,10 +170,11 @@ uint32_t gho_astar_ref8(int width, int height, const uint32_t* bitmap) {
 // and costs of gho_astar_ref8, the Manhattan heuristic (consistent: a
 // straight move costs at least 1, a diagonal one at least 2), the goal
 // (w-1, h-1) taken when popped.
-uint32_t gho_astar_grid8(int width, int height, const uint8_t* open_cells, long long* expansions) {
+uint32_t gho_astar_grid8_sg(int width, int height, const uint8_t* open_cells, int start, int goal,
+                            long long* expansions) {
     const int64_t cells = static_cast<int64_t>(width) * height;
-    const int goal = static_cast<int>(cells - 1);
-    auto heur = [&](int v) { return static_cast<uint32_t>((width - 1 - v % width) + (height - 1 - v / width)); };
+    const int tx = goal % width, ty = goal / width;
+    auto heur = [&](int v) { return static_cast<uint32_t>(std::abs(tx - v % width) + std::abs(ty - v / width)); };
     static const int kDx[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
     static const int kDy[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
     static const uint32_t kCost[8] = {3, 2, 2, 2, 1, 3, 1, 2};
@@ -181,9 +182,9 @@ uint32_t gho_astar_grid8(int width, int height, const uint8_t* open_cells, long 
     std::priority_queue<uint64_t, std::vector<uint64_t>, std::greater<uint64_t>> open;
     long long exp = 0;
     uint32_t result = 0xffffffffu;
-    if (open_cells[0] != 0 && open_cells[goal] != 0) {
-        g[0] = 0;
-        open.push(static_cast<uint64_t>(heur(0)) << 32);
+    if (open_cells[start] != 0 && open_cells[goal] != 0) {
+        g[start] = 0;
+        open.push((static_cast<uint64_t>(heur(start)) << 32) | static_cast<uint32_t>(start));
     }
     while (!open.empty()) {
         const uint64_t key = open.top();
@@ -207,6 +208,11 @@ uint32_t gho_astar_grid8(int width, int height, const uint8_t* open_cells, long 
     }
     if (expansions) *expansions = exp;
     return result;
+}
+
+uint32_t gho_astar_grid8(int width, int height, const uint8_t* open_cells, long long* expansions) {
+    return gho_astar_grid8_sg(width, height, open_cells, 0, static_cast<int>(static_cast<int64_t>(width) * height - 1),
+                              expansions);
 }
 
 uint32_t gho_astar_grid(int width, int height, const uint8_t* cost, long long* expansions, long long* max_open) {

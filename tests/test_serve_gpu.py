@@ -287,3 +287,37 @@ def test_device_loop_needs_an_idle_server(datasets):
             s.poll()  # not started
     finally:
         s.close()
+
+
+@pytest.mark.parametrize("resident", [False, True])
+def test_bitmap_maps_on_the_reference_model(datasets, resident):
+    """Maps on the reference's own model (gh_serve_add_bitmap: eight moves
+    with its direction costs) next to cost grids and graphs, through host
+    steps and through the device loop: every A* result equals the optimum
+    of the 8-neighbour oracle from its start to its goal."""
+    graphs, maps = datasets
+    rng = np.random.default_rng(44)
+    bitmaps = []
+    for k, (w, h) in enumerate([(64, 40), (300, 171), (17, 1)]):
+        o = (rng.random((h, w)) >= [0.2, 0.3, 0.0][k]).astype(np.uint8)
+        bitmaps.append(o)
+    s = new_server(graphs, maps, arena_bytes=1 << 30, max_slots=16, batch_size=256, batches_per_step=2)
+    try:
+        ids8 = [s.add_bitmap(torch.from_numpy(o).cuda()) for o in bitmaps]
+        if resident:
+            s.start(idle_ms=100)
+        qs, want = [], []
+        for j in range(24):
+            bi = j % len(bitmaps)
+            o = bitmaps[bi]
+            a, b = int(rng.integers(o.size)), int(rng.integers(o.size))
+            qs.append((gs.ASTAR, ids8[bi], a, b))
+            want.append(pyoracle.astar_grid8_sg(o, a, b))
+        mixed = make_queries(graphs, maps, 10, 45)
+        want += [w for w, _ in oracle(graphs, maps, mixed)]
+        qs += mixed
+        lat, res, _, _ = gs.run_stream(s, qs, gs.poisson_arrivals(len(qs), 500.0, 9), resident=resident)
+        assert all(r[0] == gs.FINISHED for r in res)
+        assert [r[1] for r in res] == want
+    finally:
+        s.close()
