@@ -161,38 +161,35 @@ __device__ __forceinline__ void stg_rel(int* p, int v) {
 }
 __device__ __forceinline__ int level_of(int i) { return 31 - __clz(i); }
 
+// Merge-path splits at output diagonals D and E of sorted a[0,n) and
+// b[0,n): the number of a's keys among the first D (E) outputs (a wins
+// ties).  The warp probes 32 positions per round at an odd stride, so the
+// probes of one round fall in 32 different banks; three rounds cover
+// n = 2048.  The two searches run in the same rounds.
 template <typename K>
-__device__ __forceinline__ K key_max() {
-    if constexpr (sizeof(K) == 8) return static_cast<K>(~0ull);
-    else if constexpr (static_cast<K>(-1) < static_cast<K>(0)) return static_cast<K>(0x7fffffff);
-    else return static_cast<K>(0xffffffffu);
-}
-
-// Start of the merge-path split at output diagonal D of sorted a[0,n) and
-// b[0,n): the number of a's keys among the first D outputs (a wins ties).
-// The warp probes 32 positions per round at an odd stride, so the probes of
-// one round fall in 32 different banks; three rounds cover n = 2048.
-template <typename K>
-__device__ __forceinline__ int warp_split(const K* a, const K* b, int n, int D) {
+__device__ __forceinline__ void warp_split2(const K* a, const K* b, int n, int D, int E, int& sD, int& sE) {
     const int lane = threadIdx.x & 31;
-    int L = D > n ? D - n : 0, H = D < n ? D : n;
-    while (H > L) {
-        const int step = ((H - L + 31) >> 5) | 1;
-        const int p = L + (lane + 1) * step - 1;
-        const bool t = p < H && a[p] <= b[D - 1 - p];
-        const int c = __popc(__ballot_sync(0xffffffffu, t));
-        const int nh = L + (c + 1) * step - 1;
-        L = c == 0 ? L : L + c * step;
-        H = nh < H ? nh : H;
+    int L1 = D > n ? D - n : 0, H1 = D < n ? D : n;
+    int L2 = E > n ? E - n : 0, H2 = E < n ? E : n;
+    while (H1 > L1 || H2 > L2) {
+        const int s1 = ((H1 - L1 + 31) >> 5) | 1, s2 = ((H2 - L2 + 31) >> 5) | 1;
+        const int p1 = L1 + (lane + 1) * s1 - 1, p2 = L2 + (lane + 1) * s2 - 1;
+        const bool t1 = p1 < H1 && a[p1] <= b[D - 1 - p1];
+        const bool t2 = p2 < H2 && a[p2] <= b[E - 1 - p2];
+        const int c1 = __popc(__ballot_sync(0xffffffffu, t1));
+        const int c2 = __popc(__ballot_sync(0xffffffffu, t2));
+        const int n1 = L1 + (c1 + 1) * s1 - 1, n2 = L2 + (c2 + 1) * s2 - 1;
+        L1 = c1 == 0 ? L1 : L1 + c1 * s1;
+        H1 = n1 < H1 ? n1 : H1;
+        L2 = c2 == 0 ? L2 : L2 + c2 * s2;
+        H2 = n2 < H2 ? n2 : H2;
     }
-    return L;
+    sD = L1;
+    sE = L2;
 }
 
-// One merge window: outputs [D, D + 32*IPT) of merge(a, b) into m, element
-// k = r*32 + lane in m[r].  The window's keys are the 32*IPT smallest of
-// a[i0, i0+S) and b[j0, j0+S): min(x_k, y_{S-1-k}) is that set as a
-// bitonic sequence, sorted by a bitonic network (strides >= 32 inside the
-// registers, < 32 across lanes).  Reads only shared memory.
+// Bitonic merge of the registers: a bitonic sequence over m[0..IPT) of one
+// lane comes out ascending.
 template <typename K, int IPT>
 __device__ __forceinline__ void sort_regs(K (&m)[IPT]) {
 #pragma unroll
@@ -207,28 +204,28 @@ __device__ __forceinline__ void sort_regs(K (&m)[IPT]) {
     }
 }
 
-// One merge window: outputs [D, D + 32*IPT) of merge(a, b) into m, element
-// k = r*32 + lane in m[r].  The window's keys are the 32*IPT smallest of
-// a[i0, i0+S) and b[j0, j0+S): min(x_k, y_{S-1-k}) is that set as a
-// bitonic sequence, sorted by a bitonic network.  Strides >= 32 compare
-// keys inside a lane's registers; for strides < 32, IPT = 32 transposes the
-// window through `scr` (32 x 33 keys of this warp: both access patterns hit
-// 32 different banks) so that they are inside the registers too, and back;
-// IPT = 16 uses lane shuffles.  Reads shared memory only.
+// One merge window: outputs [D, D + S) of merge(a, b), S = 32*IPT.  The
+// splits at D and D + S give the window's keys exactly: a[i0, i1) and
+// b[j0, j1), i1 - i0 + j1 - j0 = S.  Element k = r*32 + lane of the window
+// (register m[r]) is a[i0 + k] for k < i1 - i0, then b read backwards, so
+// the S keys form a bitonic sequence with one shared-memory read each;
+// a bitonic network sorts it.  Strides >= 32 compare keys inside a lane's
+// registers; for strides < 32, IPT = 32 transposes the window through `scr`
+// (32 x 33 keys of this warp: both access patterns hit 32 different banks)
+// so that they are inside the registers too, and back; IPT = 16 uses lane
+// shuffles.  Reads shared memory only.
 template <typename K, int IPT>
 __device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (&m)[IPT], K* scr) {
     constexpr int S = 32 * IPT;
     const int lane = threadIdx.x & 31;
-    const int i0 = warp_split(a, b, n, D), j0 = D - i0;
-    const K top = key_max<K>();
+    int i0, i1;
+    warp_split2(a, b, n, D, D + S, i0, i1);
+    const int na = i1 - i0, j1 = D + S - i1;
+    // element k < na: a[i0 + k]; k >= na: b[j1 - 1 - (k - na)], which is
+    // in [j0, j1) since k < S; indexed from a (both lie in one shared array)
+    const int ia = i0 + lane, ib = static_cast<int>(b - a) + (j1 - 1 + na - lane);
 #pragma unroll
-    for (int r = 0; r < IPT; ++r) {
-        const int k = r * 32 + lane;
-        const int xi = i0 + k, yi = j0 + (S - 1 - k);
-        const K x = xi < n ? a[xi] : top;
-        const K y = yi < n ? b[yi] : top;
-        m[r] = x < y ? x : y;
-    }
+    for (int r = 0; r < IPT; ++r) m[r] = a[r * 32 + lane < na ? ia + r * 32 : ib - r * 32];
     sort_regs<K, IPT>(m);
     if constexpr (IPT == 32) {
         // the sorted window stays in scr (element k at (k/32)*33 + k%32)
@@ -254,16 +251,25 @@ __device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (
     }
 }
 // Writes the window's outputs to lo[0, n) / hi[0, n) (from scr when IPT = 32).
+// A window that lies in one of the two (every one when S divides n) takes
+// one destination pointer; the one window across both (n = S/2) picks per key.
 template <typename K, int IPT>
 __device__ __forceinline__ void window_store(K* lo, K* hi, int n, int D, const K (&m)[IPT], const K* scr) {
+    constexpr int S = 32 * IPT;
     const int lane = threadIdx.x & 31;
     if constexpr (IPT == 32) __syncwarp();
+    if (D + S <= n || D >= n) {
+        K* dst = (D < n ? lo + D : hi + (D - n)) + lane;
 #pragma unroll
-    for (int r = 0; r < IPT; ++r) {
-        const int o = D + r * 32 + lane;
-        const K v = IPT == 32 ? scr[r * 33 + lane] : m[r];
-        if (o < n) lo[o] = v;
-        else hi[o - n] = v;
+        for (int r = 0; r < IPT; ++r) dst[r * 32] = IPT == 32 ? scr[r * 33 + lane] : m[r];
+    } else {
+#pragma unroll
+        for (int r = 0; r < IPT; ++r) {
+            const int o = D + r * 32 + lane;
+            const K v = IPT == 32 ? scr[r * 33 + lane] : m[r];
+            if (o < n) lo[o] = v;
+            else hi[o - n] = v;
+        }
     }
 }
 
