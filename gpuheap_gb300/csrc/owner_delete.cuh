@@ -161,11 +161,38 @@ __device__ __forceinline__ void stg_rel(int* p, int v) {
 }
 __device__ __forceinline__ int level_of(int i) { return 31 - __clz(i); }
 
+template <typename K>
+__device__ __forceinline__ K key_max() {
+    if constexpr (sizeof(K) == 8) return static_cast<K>(~0ull);
+    else if constexpr (static_cast<K>(-1) < static_cast<K>(0)) return static_cast<K>(0x7fffffff);
+    else return static_cast<K>(0xffffffffu);
+}
+
+// Start of the merge-path split at output diagonal D of sorted a[0,n) and
+// b[0,n): the number of a's keys among the first D outputs (a wins ties).
+// The warp probes 32 positions per round at an odd stride, so the probes of
+// one round fall in 32 different banks; three rounds cover n = 2048.
+template <typename K>
+__device__ __forceinline__ int warp_split(const K* a, const K* b, int n, int D) {
+    const int lane = threadIdx.x & 31;
+    int L = D > n ? D - n : 0, H = D < n ? D : n;
+    while (H > L) {
+        const int step = ((H - L + 31) >> 5) | 1;
+        const int p = L + (lane + 1) * step - 1;
+        const bool t = p < H && a[p] <= b[D - 1 - p];
+        const int c = __popc(__ballot_sync(0xffffffffu, t));
+        const int nh = L + (c + 1) * step - 1;
+        L = c == 0 ? L : L + c * step;
+        H = nh < H ? nh : H;
+    }
+    return L;
+}
+
 // Merge-path splits at output diagonals D and E of sorted a[0,n) and
 // b[0,n): the number of a's keys among the first D (E) outputs (a wins
 // ties).  The warp probes 32 positions per round at an odd stride, so the
-// probes of one round fall in 32 different banks; three rounds cover
-// n = 2048.  The two searches run in the same rounds.
+// probes of one round fall in 32 different banks.  The two searches run in
+// the same rounds.
 template <typename K>
 __device__ __forceinline__ void warp_split2(const K* a, const K* b, int n, int D, int E, int& sD, int& sE) {
     const int lane = threadIdx.x & 31;
@@ -204,28 +231,50 @@ __device__ __forceinline__ void sort_regs(K (&m)[IPT]) {
     }
 }
 
-// One merge window: outputs [D, D + S) of merge(a, b), S = 32*IPT.  The
-// splits at D and D + S give the window's keys exactly: a[i0, i1) and
-// b[j0, j1), i1 - i0 + j1 - j0 = S.  Element k = r*32 + lane of the window
-// (register m[r]) is a[i0 + k] for k < i1 - i0, then b read backwards, so
-// the S keys form a bitonic sequence with one shared-memory read each;
-// a bitonic network sorts it.  Strides >= 32 compare keys inside a lane's
-// registers; for strides < 32, IPT = 32 transposes the window through `scr`
-// (32 x 33 keys of this warp: both access patterns hit 32 different banks)
-// so that they are inside the registers too, and back; IPT = 16 uses lane
-// shuffles.  Reads shared memory only.
+// One merge window: outputs [D, D + S) of merge(a, b), S = 32*IPT, element
+// k = r*32 + lane in m[r], gathered as a bitonic sequence and sorted by a
+// bitonic network.  Two ways to gather it:
+//   * 4-byte keys with the window inside lo or hi (n >= S): one split i0 at
+//     D; the window's keys are the S smallest of the candidate runs
+//     a[i0, i0+S) and b[j0, j0+S), and min(x_k, y_{S-1-k}) is that set as a
+//     bitonic sequence (two reads a key);
+//   * otherwise: the splits at D and D + S give the window's keys exactly,
+//     a[i0, i1) and b[j0, j1); element k is a[i0 + k] for k < i1 - i0,
+//     then b read backwards (one read a key, no padding key).
+// Measured on GB300 (a window alone and in the owner's pass): the first is
+// 3-6 % faster for 4-byte keys at batch 2048, where the second split costs
+// more than the saved reads; the second is faster for 8-byte
+// keys (half the reads and registers) and for a window across lo and hi
+// (batch 512, whose splits are trivial).  Strides >= 32 compare keys inside
+// a lane's registers; for strides < 32, IPT = 32 transposes the window
+// through `scr` (32 x 33 keys of this warp: both access patterns hit 32
+// different banks) so that they are inside the registers too, and back;
+// IPT = 16 uses lane shuffles.  Reads shared memory only.
 template <typename K, int IPT>
 __device__ __forceinline__ void window(const K* a, const K* b, int n, int D, K (&m)[IPT], K* scr) {
     constexpr int S = 32 * IPT;
     const int lane = threadIdx.x & 31;
-    int i0, i1;
-    warp_split2(a, b, n, D, D + S, i0, i1);
-    const int na = i1 - i0, j1 = D + S - i1;
-    // element k < na: a[i0 + k]; k >= na: b[j1 - 1 - (k - na)], which is
-    // in [j0, j1) since k < S; indexed from a (both lie in one shared array)
-    const int ia = i0 + lane, ib = static_cast<int>(b - a) + (j1 - 1 + na - lane);
+    if (IPT == 32 && n >= S) {
+        const int i0 = warp_split(a, b, n, D), j0 = D - i0;
+        const K top = key_max<K>();
 #pragma unroll
-    for (int r = 0; r < IPT; ++r) m[r] = a[r * 32 + lane < na ? ia + r * 32 : ib - r * 32];
+        for (int r = 0; r < IPT; ++r) {
+            const int k = r * 32 + lane;
+            const int xi = i0 + k, yi = j0 + (S - 1 - k);
+            const K x = xi < n ? a[xi] : top;
+            const K y = yi < n ? b[yi] : top;
+            m[r] = x < y ? x : y;
+        }
+    } else {
+        int i0, i1;
+        warp_split2(a, b, n, D, D + S, i0, i1);
+        const int na = i1 - i0, j1 = D + S - i1;
+        // element k < na: a[i0 + k]; k >= na: b[j1 - 1 - (k - na)], which is
+        // in [j0, j1) since k < S; indexed from a (both lie in one shared array)
+        const int ia = i0 + lane, ib = static_cast<int>(b - a) + (j1 - 1 + na - lane);
+#pragma unroll
+        for (int r = 0; r < IPT; ++r) m[r] = a[r * 32 + lane < na ? ia + r * 32 : ib - r * 32];
+    }
     sort_regs<K, IPT>(m);
     if constexpr (IPT == 32) {
         // the sorted window stays in scr (element k at (k/32)*33 + k%32)
