@@ -392,6 +392,10 @@ def our_arm(args):
     t_del = [e[2].elapsed_time(e[3]) for e in evs]
     total_ms = max_over_ranks(total_ms, dist, "cuda")
 
+    # the owner's counters of the last timed step's bulk delete (the e2e
+    # steps below delete in pieces and would leave a piece's counters)
+    owner = owner_summary(h.owner_stats(), clk.summary().get("sm_mhz"))
+
     # correctness of the last step: the deleted stream is the input in key order
     if not torch.equal(out, want):
         raise SystemExit("bench: heap-sort output is not the input in key order")
@@ -427,7 +431,6 @@ def our_arm(args):
                "path": "pinned host keys -> gh_heap_sort_host (8 pieces each way, copies overlapped with the "
                        "inserts and deletes) -> pinned host output"}
 
-    owner = owner_summary(h.owner_stats(), clk.summary().get("sm_mhz"))
     value = job_rate(n, ws, args.steps, total_ms)
     ins_b, del_b = algorithmic_bytes(n, B, s, pb)
     ti, td = statistics.mean(t_ins), statistics.mean(t_del)
