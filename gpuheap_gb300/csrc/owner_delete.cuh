@@ -337,11 +337,21 @@ __device__ __forceinline__ void post_lend(OwnerCtl* oc, int node, int buf) {
 // run deleteUpdate's sift from the lent node (heap/tditdd/heap.cuh:418-532,
 // heap/buitdd/heap.cuh:403-480), which releases that node after its first
 // level -- the owner's signal that it can take it back.
+// The carried batch comes in on a barrier of its own while the sift's first
+// level takes and loads the lent node's children (the two are independent):
+// the lent node goes back to the owner one bulk load sooner.
 template <typename H, typename K>
 __device__ void owner_worker(const H& h, Mailbox* mb, const K* mdata) {
     K* base = h.region(0);
     const int B = h.batchSize;
     __shared__ int w_node, w_entry, w_q, w_exit;
+    __shared__ unsigned long long w_cbar;  // the carried batch's bulk load
+    __shared__ unsigned w_cphase;          // its parity (thread 0)
+    if (threadIdx.x == 0) {
+        detail::mbar_init(&w_cbar, 1);
+        w_cphase = 0;
+    }
+    __syncthreads();
     for (;;) {
         typename H::Op op(&h, h.ctl(base));
         if (threadIdx.x == 0) {
@@ -360,17 +370,19 @@ __device__ void owner_worker(const H& h, Mailbox* mb, const K* mdata) {
             w_entry = e;
             if (!ex) {
                 w_node = detail::ld_relaxed(&mb->node[e]);
-                op.issue(h.nodeBytes());
-                detail::bulk_g2s(base, mdata + static_cast<size_t>(e) * B, h.nodeBytes(), &op.c->bar);
+                detail::fence_proxy_async_smem();
+                detail::mbar_arrive_expect_tx(&w_cbar, h.nodeBytes());
+                detail::bulk_g2s(base, mdata + static_cast<size_t>(e) * B, h.nodeBytes(), &w_cbar);
             }
         }
         __syncthreads();
-        if (w_exit) return;
-        if (!op.wait()) return;
-        if (threadIdx.x == 0) ow::stg_rel(&mb->cons[w_entry], w_q / kMboxEntries + 1);
-        h.sift_loop(op, w_node, 0, base, base + 2 * B, base + 3 * B);
-        if (h.failed()) return;
+        if (w_exit) break;
+        CarriedInFlight cf{&w_cbar, &w_cphase, &mb->cons[w_entry], w_q / kMboxEntries + 1};
+        h.sift_loop(op, w_node, 0, base, base + 2 * B, base + 3 * B, &cf);
+        if (h.failed()) break;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) detail::mbar_inval(&w_cbar);
 }
 
 // ---------------------------------------------------------------- owner

@@ -100,6 +100,17 @@ struct OpCtl {
 };
 static_assert(sizeof(OpCtl) == 128, "OpCtl layout");
 
+// A carried batch whose bulk load is still in flight on an mbarrier of its
+// own (the owner-mode delete's workers start it before the sift's first
+// level): `phase` is thread 0's parity of `bar`; once the batch is in,
+// `cons` (global, if not null) is set to `consVal` with a release store.
+struct CarriedInFlight {
+    unsigned long long* bar;
+    unsigned* phase;
+    int* cons;
+    int consVal;
+};
+
 namespace detail {
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -1283,6 +1294,29 @@ struct Heap {
         sift_loop(op, 1, 0, C, base + 2 * B, base + 3 * B);
     }
 
+    // Block-wide: waits (bounded) for a carried batch loaded on its own
+    // barrier, then releases its source; false (block-uniform) on failure,
+    // after a second bounded wait, so that no copy lands after a return.
+    __device__ __forceinline__ bool carried_in(CarriedInFlight* cf, OpCtl* c) const {
+        if (!cf) return true;
+        if (threadIdx.x == 0) {
+            unsigned long long t0 = 0;
+            bool ok = true;
+            for (unsigned it = 0; !detail::mbar_try_wait(cf->bar, *cf->phase); ++it) {
+                if (!keep_waiting(t0, it, kSiteBulkCopy, -1, 1)) {
+                    for (unsigned i2 = 0; i2 < (1u << 22) && !detail::mbar_try_wait(cf->bar, *cf->phase); ++i2) {}
+                    ok = false;
+                    break;
+                }
+            }
+            *cf->phase ^= 1u;
+            if (ok && cf->cons) detail::st_release(cf->cons, cf->consVal);
+            if (!ok) c->abort = 1;
+        }
+        __syncthreads();
+        return !c->abort;
+    }
+
     // Sift down from `cur` (held; curPrev = the state it returns to) with the
     // carried batch in C (heap/tditdd/heap.cuh:418-532, heap/buitdd/heap.cuh:
     // 403-480).  Per level: the two lock warps take the children at once,
@@ -1290,7 +1324,12 @@ struct Heap {
     // half straight to the larger child, the case analysis against C writes
     // the current node, and one fence releases both (a second fence to free
     // the larger child before the case analysis measured slower).
-    __device__ __forceinline__ void sift_loop(Op& op, int cur, int curPrev, K* C, K* Xc, K* Yc) const {
+    //
+    // `cf` (optional): the carried batch is still in flight on a barrier of
+    // its own; the first level takes and loads the children meanwhile, then
+    // waits for both (and releases cf->cons once the carried batch is in).
+    __device__ __forceinline__ void sift_loop(Op& op, int cur, int curPrev, K* C, K* Xc, K* Yc,
+                                              CarriedInFlight* cf = nullptr) const {
         OpCtl* c = op.c;
         const int tid = threadIdx.x;
         const int B = batchSize;
@@ -1301,7 +1340,10 @@ struct Heap {
             if (tid == lockThread(0)) { int p; c->w[3] = takeChild(lv.l, p); c->w[4] = p; }
             if (tid == lockThread(1)) { int p; c->w[5] = takeChild(lv.r, p); c->w[6] = p; }
             __syncthreads();
-            if (c->w[3] < 0 || c->w[5] < 0) return;
+            if (c->w[3] < 0 || c->w[5] < 0) {
+                carried_in(cf, c);
+                return;
+            }
             lv.have = (c->w[3] == kHeld ? 1 : 0) | (c->w[5] == kHeld ? 2 : 0);
             lv.lPrev = c->w[4];
             lv.rPrev = c->w[6];
@@ -1310,7 +1352,14 @@ struct Heap {
                 if (lv.have & 1) load(Xc, lv.l, &c->bar);
                 if (lv.have & 2) load(Yc, lv.r, &c->bar);
             }
-            if (!op.wait()) return;
+            if (!op.wait()) {
+                carried_in(cf, c);
+                return;
+            }
+            if (cf) {
+                if (!carried_in(cf, c)) return;
+                cf = nullptr;
+            }
             order(lv, Xc, Yc);
             int done = 1, single = 0;
             if (lv.have == 3 && !(C[0] < (Xc[B - 1] < Yc[B - 1] ? Xc[B - 1] : Yc[B - 1]))) {
