@@ -20,8 +20,9 @@
 //     of the launch): the owner lends it the level-R node on the path
 //     together with the carried batch through a mailbox in global memory,
 //     and the worker runs deleteUpdate's sift loop from there with the
-//     usual locks; when the worker releases that node, the owner takes it
-//     back and reloads it;
+//     usual locks; when the worker is done with that node (its first level
+//     leaves the node's lock word at kLentBack), the owner takes it back
+//     and reloads it;
 //   * three control warps of the owner overlap the global latency with the
 //     merges: one takes the next delete's last node (lock, bulk load, reset
 //     to init_limits, release), one copies lends into the mailbox, one
@@ -45,6 +46,11 @@ namespace impl {
 constexpr int kMboxEntries = 32;   // lends in flight between owner and workers
 constexpr int kOwnerWarps = 29;    // compute warps of the owner block
 constexpr int kOwnerMaxR = 4;      // deepest resident level
+// Lock word a worker leaves on the lent level-R node when its first sift
+// level is done: no other lock state (TD 0-3, BU 0, 1, 2, 1 << 30), so the
+// owner's returner takes the node back on seeing it, without a CAS (no one
+// else touches a lent node during a bulk delete).
+constexpr int kLentBack = (1 << 30) + 1;
 
 // Keys per lane of a merge window: 32 for 4-byte keys (a window of 1024
 // keys, sorted with two shared-memory transposes), 16 for 8-byte keys (512,
@@ -335,8 +341,8 @@ __device__ __forceinline__ void post_lend(OwnerCtl* oc, int node, int buf) {
 // ---------------------------------------------------------------- workers
 // Blocks 1.. of the launch: take lends in order, load the carried batch and
 // run deleteUpdate's sift from the lent node (heap/tditdd/heap.cuh:418-532,
-// heap/buitdd/heap.cuh:403-480), which releases that node after its first
-// level -- the owner's signal that it can take it back.
+// heap/buitdd/heap.cuh:403-480), whose first level leaves that node's lock
+// word at kLentBack -- the owner's signal that it can take it back.
 // The carried batch comes in on a barrier of its own while the sift's first
 // level takes and loads the lent node's children (the two are independent):
 // the lent node goes back to the owner one bulk load sooner.
@@ -378,7 +384,7 @@ __device__ void owner_worker(const H& h, Mailbox* mb, const K* mdata) {
         __syncthreads();
         if (w_exit) break;
         CarriedInFlight cf{&w_cbar, &w_cphase, &mb->cons[w_entry], w_q / kMboxEntries + 1};
-        h.sift_loop(op, w_node, 0, base, base + 2 * B, base + 3 * B, &cf);
+        h.sift_loop(op, w_node, kLentBack, base, base + 2 * B, base + 3 * B, &cf);
         if (h.failed()) break;
     }
     __syncthreads();
@@ -859,7 +865,8 @@ __device__ void owner_block(const H& h, K* out, Mailbox* mb, K* mdata, int R) {
                 st = ow::lds(&oc->lentState[lane]);
                 if (st == 1) {
                     const int x = firstR + lane;
-                    if (detail::ld_relaxed(h.status + x) == 0 && detail::cas_acquire(h.status + x, 0, L) == 0) {
+                    if (detail::ld_acquire(h.status + x) == kLentBack) {
+                        h.setState(x, L);  // held by the owner again
                         detail::fence_proxy_async_smem();
                         detail::mbar_arrive_expect_tx(&oc->rbar[lane], nb);
                         h.load(slot(x - 1), x, &oc->rbar[lane]);
