@@ -30,6 +30,10 @@ modelled here at the level of those atomic steps:
   retrieve that needs the last node while an insert is still on its way
   down to it takes the insert's batch through the root instead, by the
   per-node word is_taken (0 -> 1 -> 2 -> 3 -> 0).
+* the owner-mode delete's lends (gpuheap_gb300/csrc/owner_delete.cuh): a
+  level-R node goes to a worker with the carried batch through a reused
+  mailbox entry and comes back through its lock word (kLentBack) and a
+  reload, while the owner's next plans and passes read its shared copy.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -587,3 +591,134 @@ def fifo_model(pushes=(1, 1, 1), pops=(1, 1, 1), capacity=2, wait_room=True, pub
 
     g0 = FifoState(slots=tuple([(-1, -1)] * capacity), end=0, write=0, read=0, begin=0, out=())
     return (g0, pcs), actors, final
+
+
+# --------------------------------------------------------------------------
+# the owner-mode delete's lend and return of level-R nodes
+
+LendState = namedtuple("LendState", "node_ver slot_ver lent status req seq data cons reading got")
+L_HELD, L_BACK = "L", "B"
+
+
+def _put(t, i, v):
+    return t[:i] + (v,) + t[i + 1:]
+
+
+def owner_lend_model(deletes=3, nodes=2, mark_after_pass=True, back_after_write=True, returner_checks_status=True,
+                     cons_after_load=True, lender_waits_cons=True):
+    """The lend round trip of gpuheap_gb300/csrc/owner_delete.cuh: delete d
+    lends level-R node d % `nodes` (with nodes = 1 every path runs through
+    the same node, the common case; with 2 a lend can go out while the
+    previous node is still away), through one mailbox entry that
+    consecutive lends reuse.
+
+    * `owner` (the compute warps), per delete d with x = d % nodes: the plan
+      waits until lentState[x] is 0 and reads x's shared slot; it posts lend
+      d (x and the carried batch); the pass reads the slot (two steps); only
+      then lentState[x] = 1.
+    * `lender`: copies lend q's carried batch into the mailbox entry once
+      the worker has read lend q - 1 from it (cons), then publishes seq.
+    * `worker`: takes lend q when seq says so and starts the carried batch's
+      bulk load; when the load is in it releases cons (CarriedInFlight),
+      writes x's new content to global memory and leaves x's lock word at
+      kLentBack.
+    * `returner`: for a node with lentState 1 and lock word kLentBack, sets
+      the word back to held, reloads the slot from global memory (the bulk
+      copy takes the node's version at that moment), then lentState = 0.
+
+    Invariants: a plan reads its node's current version; no reload lands
+    while the pass reads that slot; the worker's carried batch is its own
+    lend's; at the end every version matches, every node is held and every
+    lend was received once.  Planted mistakes: lentState set before the
+    pass, kLentBack before the write, a returner that does not look at the
+    lock word, cons released when the load starts, a lender that does not
+    wait for cons."""
+
+    def owner(g, pc, trace):
+        step, d = pc
+        x = d % nodes
+        if step == "plan":
+            if g.lent[x] != 0:
+                return []
+            if g.slot_ver[x] != g.node_ver[x]:
+                raise Violation(f"plan {d} read node {x}'s slot at version {g.slot_ver[x]}, the node is at "
+                                f"{g.node_ver[x]}", list(trace) + [f"owner:plan {d}"])
+            return [(f"plan {d}", g, ("post", d))]
+        if step == "post":
+            nxt = ("pass_start", d) if mark_after_pass else ("early_mark", d)
+            return [(f"post lend {d} (node {x})", _set(g, req=d + 1), nxt)]
+        if step == "early_mark":
+            return [(f"lentState[{x}] 1 before the pass", _set(g, lent=_put(g.lent, x, 1)), ("pass_start", d))]
+        if step == "pass_start":
+            return [(f"pass {d} reads node {x}'s slot", _set(g, reading=x), ("pass_end", d))]
+        if step == "pass_end":
+            nxt = ("mark", d) if mark_after_pass else ("next", d)
+            return [(f"pass {d} done", _set(g, reading=-1), nxt)]
+        if step == "mark":
+            return [(f"lentState[{x}] 1", _set(g, lent=_put(g.lent, x, 1)), ("next", d))]
+        if step == "next":
+            return [("next delete", g, ("plan", d + 1) if d + 1 < deletes else None)]
+        return []
+
+    def lender(g, pc, trace):
+        q = pc
+        if g.req <= q:
+            return []
+        if lender_waits_cons and g.cons != q:
+            return []
+        return [(f"copies lend {q} into the entry, seq {q + 1}", _set(g, data=q, seq=q + 1),
+                 q + 1 if q + 1 < deletes else None)]
+
+    def worker(g, pc, trace):
+        step, q = pc
+        x = q % nodes
+        nxt_lend = ("take", q + 1) if q + 1 < deletes else None
+        if step == "take":
+            if g.seq != q + 1:
+                return []
+            g2 = g if cons_after_load else _set(g, cons=q + 1)
+            return [(f"takes lend {q}, starts the carried load", g2, ("load_end", q))]
+        if step == "load_end":
+            if g.data != q:
+                raise Violation(f"worker's carried batch for lend {q} is lend {g.data}'s",
+                                list(trace) + [f"worker:load_end {q}"])
+            g2 = _set(g, cons=q + 1) if cons_after_load else g
+            return [(f"carried batch {q} in", _set(g2, got=g.got + 1), ("write", q))]
+        if step == "write":
+            if back_after_write:
+                return [(f"writes node {x}", _set(g, node_ver=_put(g.node_ver, x, g.node_ver[x] + 1)), ("back", q))]
+            return [(f"node {x} kLentBack before the write", _set(g, status=_put(g.status, x, L_BACK)),
+                     ("late_write", q))]
+        if step == "late_write":
+            return [(f"writes node {x}", _set(g, node_ver=_put(g.node_ver, x, g.node_ver[x] + 1)), nxt_lend)]
+        if step == "back":
+            return [(f"node {x} kLentBack", _set(g, status=_put(g.status, x, L_BACK)), nxt_lend)]
+        return []
+
+    def returner(g, pc, trace):
+        k = pc  # reloads done
+        moves = []
+        for x in range(nodes):
+            if g.lent[x] != 1 or (returner_checks_status and g.status[x] != L_BACK):
+                continue
+            if g.reading == x:
+                raise Violation(f"reload of node {x} lands while the pass reads its slot",
+                                list(trace) + [f"returner:reload {x}"])
+            g2 = _set(g, status=_put(g.status, x, L_HELD), slot_ver=_put(g.slot_ver, x, g.node_ver[x]),
+                      lent=_put(g.lent, x, 0))
+            moves.append((f"takes node {x} back at version {g.node_ver[x]}", g2, k + 1 if k + 1 < deletes else None))
+        return moves
+
+    def final(g, trace):
+        if g.got != deletes:
+            raise Violation(f"worker received {g.got} carried batches of {deletes}", trace)
+        per = [deletes // nodes + (1 if x < deletes % nodes else 0) for x in range(nodes)]
+        if list(g.node_ver) != per or list(g.slot_ver) != per or any(g.lent) or \
+                any(st != L_HELD for st in g.status):
+            raise Violation(f"end: nodes at {g.node_ver}, slots at {g.slot_ver}, lentState {g.lent}, "
+                            f"lock words {g.status}", trace)
+
+    z = (0,) * nodes
+    g0 = LendState(node_ver=z, slot_ver=z, lent=z, status=(L_HELD,) * nodes, req=0, seq=0, data=-1, cons=0,
+                   reading=-1, got=0)
+    return (g0, (("plan", 0), 0, ("take", 0), 0)), [owner, lender, worker, returner], final

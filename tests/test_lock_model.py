@@ -1,7 +1,8 @@
 """Race detection for the path's lock-free protocols, on CPU: every
 interleaving of the atomic steps of the bottom-up park protocol, the
-top-down target hand-off, the FIFO ring and the searches' termination
-protocol (oracle/lock_model.py) keeps its invariants and never deadlocks,
+top-down target hand-off, the FIFO ring, the searches' termination
+protocol, the retrieving heap's steal and the owner-mode delete's lends
+(oracle/lock_model.py) keeps its invariants and never deadlocks,
 and the explorer finds each planted mistake -- the ones these protocols
 exist to prevent -- with the interleaving that exposes it."""
 import pytest
@@ -159,3 +160,27 @@ def test_retrieve_steal_planted_mistakes_are_caught(mistake):
     except lm.Violation:
         return
     assert res.deadlocks, f"{mistake}: no violation and no deadlock found"
+
+
+# ------------------------------------------------ owner-mode lend and return
+@pytest.mark.parametrize("deletes,nodes", [(2, 1), (3, 1), (3, 2), (4, 2), (5, 3)])
+def test_owner_lend_round_trip_is_safe(deletes, nodes):
+    """The owner lends a level-R node with the carried batch, the worker's
+    first level rewrites it and leaves kLentBack, the returner reloads it:
+    every plan reads the node's current version, no reload lands during a
+    pass, every carried batch reaches its own lend."""
+    res = _run(lm.owner_lend_model(deletes=deletes, nodes=nodes))
+    assert res.deadlocks == [] and res.finals == 1
+
+
+@pytest.mark.parametrize("mistake,found", [
+    ("mark_after_pass", "lands while the pass reads"),
+    ("back_after_write", "slots at"),
+    ("returner_checks_status", "lock words"),
+    ("cons_after_load", "carried batch for lend"),
+    ("lender_waits_cons", "carried batch for lend"),
+])
+def test_owner_lend_planted_mistakes_are_caught(mistake, found):
+    with pytest.raises(lm.Violation) as e:
+        _run(lm.owner_lend_model(deletes=4, nodes=2, **{mistake: False}))
+    assert found in str(e.value)
