@@ -33,7 +33,9 @@ modelled here at the level of those atomic steps:
 * the owner-mode delete's lends (gpuheap_gb300/csrc/owner_delete.cuh): a
   level-R node goes to a worker with the carried batch through a reused
   mailbox entry and comes back through its lock word (kLentBack) and a
-  reload, while the owner's next plans and passes read its shared copy.
+  reload, while the owner's next plans and passes read its shared copy;
+  the taker loads each delete's last node into one of two buffers one
+  delete ahead, and a buffer is loaded again only when its reads are over.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -722,3 +724,100 @@ def owner_lend_model(deletes=3, nodes=2, mark_after_pass=True, back_after_write=
     g0 = LendState(node_ver=z, slot_ver=z, lent=z, status=(L_HELD,) * nodes, req=0, seq=0, data=-1, cons=0,
                    reading=-1, got=0)
     return (g0, (("plan", 0), 0, ("take", 0), 0)), [owner, lender, worker, returner], final
+
+
+# --------------------------------------------------------------------------
+# the owner-mode delete's two carried-batch buffers
+
+TakerState = namedtuple("TakerState", "buf ready free allowed computing copying req done_lends")
+
+
+def owner_taker_model(deletes=4, lends=(True, False, True, True), taker_waits_free=True, free_after_copy=True,
+                      compute_waits_ready=True):
+    """The carried-batch buffers of gpuheap_gb300/csrc/owner_delete.cuh: the
+    taker warp takes delete t's last node into buffer t & 1 one delete
+    ahead; delete d's compute warps read buffer d & 1 (refill, plan, general
+    steps) and, when d lends its level-R node, the lender warp copies the
+    buffer into the mailbox afterwards.
+
+    * `taker`, per t: waits until takeAllowed > t and cFree[b] >= t >> 1
+      (both earlier uses of the buffer are over), loads the node into the
+      buffer, cReady[b] = t + 1.
+    * `compute`, per d: waits for cReady[b] == d + 1, sets takeAllowed =
+      d + 2, reads the buffer (two steps); a lending delete posts the
+      request for the lender (whose copy then frees the buffer), any other
+      frees it itself (cFree[b] += 1).
+    * `lender`: copies the buffer of each posted lend (two steps), then
+      cFree[b] += 1.
+
+    Invariants: every read finds its own delete's last node and no load
+    lands in a buffer that is being read.  Planted mistakes: a taker that
+    does not wait for cFree, a lending delete that frees the buffer itself
+    (before the lender's copy), compute warps that do not wait for cReady."""
+    assert len(lends) == deletes
+
+    def taker(g, pc, trace):
+        t = pc
+        b = t & 1
+        if g.allowed <= t:
+            return []
+        if taker_waits_free and g.free[b] < (t >> 1):
+            return []
+        if g.computing == b or g.copying == b:
+            raise Violation(f"take {t} loads buffer {b} while it is read", list(trace) + [f"taker:load {t}"])
+        g2 = _set(g, buf=_put(g.buf, b, t), ready=_put(g.ready, b, t + 1))
+        return [(f"loads delete {t}'s last node into buffer {b}", g2, t + 1 if t + 1 < deletes else None)]
+
+    def compute(g, pc, trace):
+        step, d = pc
+        b = d & 1
+        if step == "wait":
+            if compute_waits_ready and g.ready[b] != d + 1:
+                return []
+            return [(f"delete {d}: buffer {b} ready", _set(g, allowed=max(g.allowed, d + 2)), ("read", d))]
+        if step == "read":
+            if g.buf[b] != d:
+                raise Violation(f"delete {d} reads buffer {b} holding delete {g.buf[b]}'s node",
+                                list(trace) + [f"compute:read {d}"])
+            return [(f"delete {d} reads buffer {b}", _set(g, computing=b), ("done", d))]
+        if step == "done":
+            g2 = _set(g, computing=-1)
+            nxt = ("wait", d + 1) if d + 1 < deletes else None
+            if lends[d]:
+                g2 = _set(g2, req=g2.req + (d,))
+                if not free_after_copy:
+                    g2 = _set(g2, free=_put(g2.free, b, g2.free[b] + 1))
+                return [(f"delete {d} posts its lend", g2, nxt)]
+            return [(f"delete {d} frees buffer {b}", _set(g2, free=_put(g2.free, b, g2.free[b] + 1)), nxt)]
+        return []
+
+    def lender(g, pc, trace):
+        step, k = pc  # k = lends copied
+        total = sum(lends)
+        if step == "wait":
+            if len(g.req) <= k:
+                return []
+            d = g.req[k]
+            b = d & 1
+            if g.buf[b] != d:
+                raise Violation(f"lend of delete {d} copies buffer {b} holding delete {g.buf[b]}'s node",
+                                list(trace) + [f"lender:copy {d}"])
+            return [(f"copies delete {d}'s buffer {b}", _set(g, copying=b), ("free", k))]
+        if step == "free":
+            d = g.req[k]
+            b = d & 1
+            g2 = _set(g, copying=-1, done_lends=g.done_lends + 1)
+            if free_after_copy:
+                g2 = _set(g2, free=_put(g2.free, b, g2.free[b] + 1))
+            return [(f"copied, frees buffer {b}", g2, ("wait", k + 1) if k + 1 < total else None)]
+        return []
+
+    def final(g, trace):
+        if g.done_lends != sum(lends):
+            raise Violation(f"{g.done_lends} lends copied of {sum(lends)}", trace)
+
+    g0 = TakerState(buf=(-1, -1), ready=(0, 0), free=(0, 0), allowed=1, computing=-1, copying=-1, req=(),
+                    done_lends=0)
+    actors = [taker, compute] + ([lender] if any(lends) else [])
+    pcs = (0, ("wait", 0)) + ((("wait", 0),) if any(lends) else ())
+    return (g0, pcs), actors, final

@@ -184,3 +184,23 @@ def test_owner_lend_planted_mistakes_are_caught(mistake, found):
     with pytest.raises(lm.Violation) as e:
         _run(lm.owner_lend_model(deletes=4, nodes=2, **{mistake: False}))
     assert found in str(e.value)
+
+
+@pytest.mark.parametrize("lends", [(True, False, True, True), (True,) * 5, (False,) * 4, (False, True, True, False, True)])
+def test_owner_carried_buffers_are_safe(lends):
+    """The taker loads the next delete's last node into the other buffer;
+    a buffer is loaded again only after its delete and, when it lent, the
+    lender's copy are done."""
+    res = _run(lm.owner_taker_model(deletes=len(lends), lends=lends))
+    assert res.deadlocks == [] and res.finals == 1
+
+
+@pytest.mark.parametrize("mistake,found", [
+    ("taker_waits_free", "while it is read"),
+    ("free_after_copy", "while it is read"),
+    ("compute_waits_ready", "holding delete"),
+])
+def test_owner_carried_buffer_mistakes_are_caught(mistake, found):
+    with pytest.raises(lm.Violation) as e:
+        _run(lm.owner_taker_model(**{mistake: False}))
+    assert found in str(e.value)
