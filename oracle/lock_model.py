@@ -36,6 +36,11 @@ modelled here at the level of those atomic steps:
   reload, while the owner's next plans and passes read its shared copy;
   the taker loads each delete's last node into one of two buffers one
   delete ahead, and a buffer is loaded again only when its reads are over.
+* the served device loop's token queue (gpuheap_gb300/csrc/
+  search_kernels.cuh, namespace sv): a bounded multi-producer
+  multi-consumer ring of per-cell sequence words carries a query's setup
+  and search tokens, and the block that retires the last token completes
+  the query.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -821,3 +826,137 @@ def owner_taker_model(deletes=4, lends=(True, False, True, True), taker_waits_fr
     actors = [taker, compute] + ([lender] if any(lends) else [])
     pcs = (0, ("wait", 0)) + ((("wait", 0),) if any(lends) else ())
     return (g0, pcs), actors, final
+
+
+# --------------------------------------------------------------------------
+# the served device loop's token queue and a query's retirement
+
+TokenState = namedtuple("TokenState", "cells enq deq tokens over stints completed setups")
+SETUP, SEARCH = "setup", "search"
+
+
+def serve_token_model(blocks=2, query_blocks=2, cells=2, max_stints=3, pop_by_cas=True, push_waits_cell=True,
+                      release_after_read=True, retire_atomic=True):
+    """The served loop's token queue and retirement (search_kernels.cuh,
+    namespace sv: `push`, `pop`, `setup_query`, `end_stint`): a bounded
+    multi-producer multi-consumer ring in which cell c serves positions
+    c, c + cells, ...; its sequence word is pos when free for position pos,
+    pos + 1 when holding pos's token.
+
+    * push: pos = atomicAdd(enq); wait until seq == pos; write the token;
+      seq = pos + 1 (release).
+    * pop: read deq, then the cell's seq; seq == pos + 1: CAS deq pos ->
+      pos + 1, on success read the token and free the cell for pos + cells
+      (seq = pos + cells); seq < pos + 1: empty.
+    * One query: the admission queued its setup token; the block that pops
+      it pushes `query_blocks` search tokens.  A block with a search token
+      works a stint; if the search is not over (it may end at any stint,
+      and does after `max_stints`) the token goes back, else the block
+      decrements the query's token count and the one that takes it to 0
+      completes the query.
+
+    A block polling an empty ring is a wait (the loop's stall limit would
+    end it), so a query whose tokens are all gone without a completion
+    shows up as a deadlock.  Invariants: a pop reads the token pushed for
+    its position; the query completes exactly once, after every token has
+    retired; the ring ends empty.  Planted mistakes: claiming by a plain store instead of a CAS, a
+    push that does not wait for its cell, a cell freed before its token is
+    read, and a retirement by load and store instead of atomicSub."""
+
+    def put(g, pos, val):
+        cs = list(g.cells)
+        cs[pos % cells] = (pos + 1, (pos, val))
+        return _set(g, cells=tuple(cs))
+
+    def block(i):
+        def act(g, pc, trace):
+            kind = pc[0]
+            if kind == "next":
+                if g.completed:
+                    return [("leaves", g, None)]
+                if g.deq >= g.enq:
+                    return []  # nothing queued: polls until a token comes (or the loop's stall limit)
+                return [(f"reads deq {g.deq}", g, ("seq", g.deq))]
+            if kind == "seq":
+                pos = pc[1]
+                s, _ = g.cells[pos % cells]
+                if s == pos + 1:
+                    return [(f"cell {pos % cells} holds {pos}", g, ("cas", pos))]
+                return [("empty", g, ("next",))]
+            if kind == "cas":
+                pos = pc[1]
+                if pop_by_cas and g.deq != pos:
+                    return [("cas lost", g, ("next",))]
+                g2 = _set(g, deq=pos + 1 if pop_by_cas else max(g.deq, pos + 1))
+                if release_after_read:
+                    return [(f"claims {pos}", g2, ("read", pos))]
+                cs = list(g2.cells)
+                cs[pos % cells] = (pos + cells, cs[pos % cells][1])
+                return [(f"claims {pos}, frees its cell first", _set(g2, cells=tuple(cs)), ("read", pos))]
+            if kind == "read":
+                pos = pc[1]
+                _, (wpos, val) = g.cells[pos % cells]
+                if wpos != pos:
+                    raise Violation(f"block {i} popped position {pos} and read position {wpos}'s token",
+                                    list(trace) + [f"b{i}:read {pos}"])
+                g2 = g
+                if release_after_read:
+                    cs = list(g.cells)
+                    cs[pos % cells] = (pos + cells, (wpos, val))
+                    g2 = _set(g, cells=tuple(cs))
+                return [(f"takes {val}", g2, ("got", val))]
+            if kind == "got":
+                val = pc[1]
+                if val == SETUP:
+                    if g.setups:
+                        raise Violation("the setup token ran twice", list(trace) + [f"b{i}:setup"])
+                    return [("sets the query up", _set(g, setups=1), ("push", SEARCH, query_blocks))]
+                # a stint; the search may end here
+                moves = []
+                if not g.over and g.stints < max_stints:
+                    moves.append(("stint, search goes on", _set(g, stints=g.stints + 1), ("push", SEARCH, 1)))
+                moves.append(("stint, search over", _set(g, over=True, stints=g.stints + 1), ("retire",)))
+                if g.over:
+                    moves = [("stint, search over", g, ("retire",))]
+                return moves
+            if kind == "push":
+                _, val, left = pc
+                if left == 0:
+                    return [("pushed", g, ("next",))]
+                pos = g.enq
+                return [(f"reserves {pos}", _set(g, enq=pos + 1), ("wait", val, left, pos))]
+            if kind == "wait":
+                _, val, left, pos = pc
+                s, _ = g.cells[pos % cells]
+                if push_waits_cell and s != pos:
+                    return []
+                return [(f"writes {val} at {pos}", put(g, pos, val), ("push", val, left - 1))]
+            if kind == "retire":
+                if retire_atomic:
+                    left = g.tokens - 1
+                    g2 = _set(g, tokens=left)
+                    if left == 0:
+                        return [("last token: completes", _set(g2, completed=g2.completed + 1), ("next",))]
+                    return [(f"token retires ({left} left)", g2, ("next",))]
+                return [(f"reads tokens {g.tokens}", g, ("retire_w", g.tokens))]
+            if kind == "retire_w":
+                left = pc[1] - 1
+                g2 = _set(g, tokens=left)
+                if left == 0:
+                    return [("writes 0: completes", _set(g2, completed=g2.completed + 1), ("next",))]
+                return [(f"writes {left}", g2, ("next",))]
+            return []
+        act.__name__ = f"b{i}"
+        return act
+
+    def final(g, trace):
+        if g.completed != 1 or g.tokens != 0:
+            raise Violation(f"query completed {g.completed} times, {g.tokens} tokens out", trace)
+        if g.deq != g.enq:
+            raise Violation(f"ring ends with deq {g.deq}, enq {g.enq}", trace)
+
+    c0 = [(k, (-1, None)) for k in range(cells)]
+    c0[0] = (1, (0, SETUP))  # the admission's setup token at position 0
+    g0 = TokenState(cells=tuple(c0), enq=1, deq=0, tokens=query_blocks, over=False, stints=0, completed=0,
+                    setups=0)
+    return (g0, tuple(("next",) for _ in range(blocks))), [block(i) for i in range(blocks)], final

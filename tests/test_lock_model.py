@@ -204,3 +204,31 @@ def test_owner_carried_buffer_mistakes_are_caught(mistake, found):
     with pytest.raises(lm.Violation) as e:
         _run(lm.owner_taker_model(**{mistake: False}))
     assert found in str(e.value)
+
+
+# ------------------------------------------------ served loop's token queue
+@pytest.mark.parametrize("blocks,query_blocks,cells,stints", [(2, 2, 2, 3), (3, 2, 2, 2), (2, 3, 3, 2)])
+def test_serve_token_queue_is_safe(blocks, query_blocks, cells, stints):
+    """Every pop reads its own position's token, the query completes once
+    after all its tokens retired, the ring ends empty, nobody waits forever."""
+    res = _run(lm.serve_token_model(blocks=blocks, query_blocks=query_blocks, cells=cells, max_stints=stints))
+    assert res.deadlocks == [] and res.finals >= 1
+
+
+@pytest.mark.parametrize("mistake,found", [
+    ("pop_by_cas", "tokens out"),
+    ("push_waits_cell", "read position"),
+    ("release_after_read", "read position"),
+])
+def test_serve_token_queue_mistakes_are_caught(mistake, found):
+    with pytest.raises(lm.Violation) as e:
+        _run(lm.serve_token_model(**{mistake: False}))
+    assert found in str(e.value)
+
+
+def test_serve_retire_by_load_and_store_loses_the_completion():
+    """Two blocks retire the last two tokens by load and store: both write
+    1, nobody completes the query and every block waits on an empty ring."""
+    res = _run(lm.serve_token_model(retire_atomic=False))
+    assert res.deadlocks
+    assert any(t.startswith("b0:reads tokens 2") or t.startswith("b1:reads tokens 2") for t in res.deadlocks[0])
