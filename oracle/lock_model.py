@@ -40,7 +40,7 @@ modelled here at the level of those atomic steps:
   search_kernels.cuh, namespace sv): a bounded multi-producer
   multi-consumer ring of per-cell sequence words carries a query's setup
   and search tokens, and the block that retires the last token completes
-  the query.
+  the query; requests and completions cross in rings in pinned host memory.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -960,3 +960,135 @@ def serve_token_model(blocks=2, query_blocks=2, cells=2, max_stints=3, pop_by_ca
     g0 = TokenState(cells=tuple(c0), enq=1, deq=0, tokens=query_blocks, over=False, stints=0, completed=0,
                     setups=0)
     return (g0, tuple(("next",) for _ in range(blocks))), [block(i) for i in range(blocks)], final
+
+
+# --------------------------------------------------------------------------
+# the served device loop's request and completion rings (pinned host memory)
+
+RingState = namedtuple("RingState", "req posted taken admitted claim done consumed claimed")
+
+
+def serve_rings_model(queries=4, cap=2, completers=2, guard_by_completions=True, seq_after_fields=True,
+                      take_after_copy=True):
+    """The host <-> device rings of the served loop (gpuheap_gb300/csrc/
+    serve.cu `post_requests`, `gh_serve_poll`; search_kernels.cuh `admit`,
+    `complete`).  Both rings have `cap` records; record k of a ring holds
+    item k when its seq word is k + 1.
+
+    * `host`: posts request p into record p % cap (fields, then seq with a
+      release store) while p - consumed < cap, consumed counting the
+      completions it has read; reads completion c when its seq is c + 1.
+    * `admit` (device, lock held): copies request `taken` when its seq says
+      so, then publishes taken + 1; the query is then active.
+    * `complete` x `completers` (device blocks): any active query may end
+      next; its block claims completion number c (lock held), writes the
+      record's fields, then its seq.
+
+    Invariants: the device copies the request posted for that number; the
+    host reads completion c as the query claimed with c; no completion
+    record is written while the host has yet to read the one it replaces;
+    every query completes.  Planted mistakes: posting while p - taken < cap
+    (counting admissions instead of completions) and a completion's seq
+    written before its fields.  `take_after_copy=False` publishes taken
+    before the copy: still safe, because the host reuses a request record
+    only after that request's completion (taken is only reported)."""
+
+    def host(g, pc, trace):
+        moves = []
+        step = pc[0]
+        if step == "idle":
+            limit = g.consumed if guard_by_completions else g.taken
+            if g.posted < queries and g.posted - limit < cap:
+                p = g.posted
+                req = list(g.req)
+                req[p % cap] = (req[p % cap][0], p)  # fields
+                moves.append((f"writes request {p}", _set(g, req=tuple(req)), ("publish", p)))
+            c = g.consumed
+            if c < queries and g.done[c % cap][0] == c + 1:
+                qid = g.done[c % cap][1]
+                if qid != g.claimed[c]:
+                    raise Violation(f"host read completion {c} as query {qid}, claimed by query {g.claimed[c]}",
+                                    list(trace) + [f"host:read {c}"])
+                nxt = "idle" if c + 1 < queries else None
+                moves.append((f"reads completion {c} (query {qid})", _set(g, consumed=c + 1), (nxt,) if nxt else None))
+            return moves
+        if step == "publish":
+            p = pc[1]
+            req = list(g.req)
+            req[p % cap] = (p + 1, req[p % cap][1])
+            return [(f"publishes request {p}", _set(g, req=tuple(req), posted=p + 1), ("idle",))]
+        return []
+
+    def admit(g, pc, trace):
+        t = g.taken
+        if t >= queries or g.req[t % cap][0] != t + 1:
+            return []
+        if take_after_copy:
+            content = g.req[t % cap][1]
+            if content != t:
+                raise Violation(f"device copied request {t} and found request {content}'s fields",
+                                list(trace) + [f"admit:copy {t}"])
+            return [(f"copies request {t}, taken {t + 1}", _set(g, taken=t + 1, admitted=g.admitted + (t,)),
+                     "idle" if t + 1 < queries else None)]
+        return [(f"taken {t + 1} before the copy", _set(g, taken=t + 1), ("late_copy", t))]
+
+    def admit_wrap(g, pc, trace):
+        if pc == "idle":
+            return admit(g, pc, trace)
+        if isinstance(pc, tuple) and pc[0] == "late_copy":
+            t = pc[1]
+            content = g.req[t % cap][1]
+            if content != t:
+                raise Violation(f"device copied request {t} and found request {content}'s fields",
+                                list(trace) + [f"admit:late copy {t}"])
+            return [(f"copies request {t}", _set(g, admitted=g.admitted + (t,)),
+                     "idle" if t + 1 < queries else None)]
+        return []
+    admit_wrap.__name__ = "admit"
+
+    def completer(k):
+        def act(g, pc, trace):
+            if pc == "idle":
+                moves = []
+                for q in g.admitted:
+                    c = g.claim
+                    claimed = g.claimed[:c] + (q,) + g.claimed[c + 1:]
+                    left = tuple(x for x in g.admitted if x != q)
+                    moves.append((f"query {q} ends, claims completion {c}",
+                                  _set(g, admitted=left, claim=c + 1, claimed=claimed), ("write", c, q)))
+                if g.claim >= queries:
+                    return [("leaves", g, None)]
+                return moves
+            step, c, q = pc
+            slot = c % cap
+            if step == "write":
+                old_seq = g.done[slot][0]
+                if old_seq != 0 and old_seq - 1 >= g.consumed:
+                    raise Violation(f"completion {c} overwrites completion {old_seq - 1} before the host read it",
+                                    list(trace) + [f"c{k}:write {c}"])
+                done = list(g.done)
+                if seq_after_fields:
+                    done[slot] = (old_seq, q)
+                    return [(f"writes completion {c}'s fields", _set(g, done=tuple(done)), ("seq", c, q))]
+                done[slot] = (c + 1, done[slot][1])
+                return [(f"completion {c}: seq first", _set(g, done=tuple(done)), ("late_fields", c, q))]
+            if step == "seq":
+                done = list(g.done)
+                done[slot] = (c + 1, done[slot][1])
+                return [(f"publishes completion {c}", _set(g, done=tuple(done)), "idle")]
+            if step == "late_fields":
+                done = list(g.done)
+                done[slot] = (done[slot][0], q)
+                return [(f"writes completion {c}'s fields", _set(g, done=tuple(done)), "idle")]
+            return []
+        act.__name__ = f"c{k}"
+        return act
+
+    def final(g, trace):
+        if g.consumed != queries or g.admitted:
+            raise Violation(f"host read {g.consumed} of {queries} completions, {len(g.admitted)} still active", trace)
+
+    g0 = RingState(req=tuple((0, -1) for _ in range(cap)), posted=0, taken=0, admitted=(), claim=0,
+                   done=tuple((0, -1) for _ in range(cap)), consumed=0, claimed=(-1,) * queries)
+    actors = [host, admit_wrap] + [completer(k) for k in range(completers)]
+    return (g0, (("idle",), "idle") + ("idle",) * completers), actors, final

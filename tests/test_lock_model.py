@@ -232,3 +232,29 @@ def test_serve_retire_by_load_and_store_loses_the_completion():
     res = _run(lm.serve_token_model(retire_atomic=False))
     assert res.deadlocks
     assert any(t.startswith("b0:reads tokens 2") or t.startswith("b1:reads tokens 2") for t in res.deadlocks[0])
+
+
+# ------------------------------------------------ served loop's host rings
+@pytest.mark.parametrize("queries,cap,completers", [(4, 2, 2), (5, 2, 2), (4, 3, 3)])
+def test_serve_rings_are_safe(queries, cap, completers):
+    """Requests out through pinned memory, completions back in any order of
+    ending: every record is read as written, none is overwritten unread."""
+    res = _run(lm.serve_rings_model(queries=queries, cap=cap, completers=completers))
+    assert res.deadlocks == [] and res.finals >= 1
+
+
+@pytest.mark.parametrize("mistake,found", [
+    ("guard_by_completions", "before the host read it"),
+    ("seq_after_fields", "host read completion"),
+])
+def test_serve_rings_mistakes_are_caught(mistake, found):
+    with pytest.raises(lm.Violation) as e:
+        _run(lm.serve_rings_model(**{mistake: False}))
+    assert found in str(e.value)
+
+
+def test_serve_rings_taken_is_advisory():
+    """The host reuses a request record only after its completion, so the
+    device may publish `taken` before its copy without harm."""
+    res = _run(lm.serve_rings_model(take_after_copy=False))
+    assert res.deadlocks == [] and res.finals >= 1
