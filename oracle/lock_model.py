@@ -69,25 +69,40 @@ class Result:
     states: int = 0
     finals: int = 0
     deadlocks: list = field(default_factory=list)
+    stuck: list = field(default_factory=list)  # (with progress=True) states that can never finish
 
 
-def explore(initial, actors, check_final=None, limit=2_000_000):
+def explore(initial, actors, check_final=None, limit=2_000_000, progress=False):
     """Depth-first search over every interleaving.  `initial` is a tuple
     (global state, one program counter per actor); each actor is a function
     (state, pc) -> list of (label, new_state, new_pc), empty when it is
     blocked or done (pc None).  `check_final(state)` runs at every state
     where all actors are done.  Raises Violation from an actor step or the
     final check; returns the number of states and any deadlocks (with the
-    trace that reached them)."""
+    trace that reached them).
+
+    With `progress`, the explorer also keeps the state graph and reports in
+    `stuck` the states from which no final state can be reached (traces of
+    up to three): a livelock, where actors keep moving in a cycle that
+    never ends, shows up there though no state is a deadlock."""
     res = Result()
     seen = set()
-    stack = [(initial, ())]
+    succ = {} if progress else None
+    parent = {} if progress else None
+    finals = []
+    stack = [(initial, (), None)]
     while stack:
-        (g, pcs), trace = stack.pop()
+        (g, pcs), trace, par = stack.pop()
         key = (g, pcs)
         if key in seen:
+            if progress and par is not None:
+                succ.setdefault(par, set()).add(key)
             continue
         seen.add(key)
+        if progress:
+            if par is not None:
+                succ.setdefault(par, set()).add(key)
+            parent[key] = trace
         res.states += 1
         if res.states > limit:
             raise RuntimeError("state space larger than the limit")
@@ -100,6 +115,7 @@ def explore(initial, actors, check_final=None, limit=2_000_000):
         if not moves:
             if all(pc is None for pc in pcs):
                 res.finals += 1
+                finals.append(key)
                 if check_final:
                     check_final(g, list(trace))
             else:
@@ -107,7 +123,23 @@ def explore(initial, actors, check_final=None, limit=2_000_000):
             continue
         for i, label, g2, pc2 in moves:
             pcs2 = pcs[:i] + (pc2,) + pcs[i + 1:]
-            stack.append(((g2, pcs2), trace + (f"{actors[i].__name__}:{label}",)))
+            stack.append(((g2, pcs2), trace + (f"{actors[i].__name__}:{label}",), key))
+    if progress:
+        pred = {}
+        for a, bs in succ.items():
+            for b in bs:
+                pred.setdefault(b, []).append(a)
+        live = set(finals)
+        work = list(finals)
+        while work:
+            b = work.pop()
+            for a in pred.get(b, ()):
+                if a not in live:
+                    live.add(a)
+                    work.append(a)
+        dead = [k for k in seen if k not in live]
+        dead.sort(key=lambda k: len(parent[k]))
+        res.stuck = [list(parent[k]) for k in dead[:3]]
     return res
 
 
@@ -836,7 +868,7 @@ SETUP, SEARCH = "setup", "search"
 
 
 def serve_token_model(blocks=2, query_blocks=2, cells=2, max_stints=3, pop_by_cas=True, push_waits_cell=True,
-                      release_after_read=True, retire_atomic=True):
+                      release_after_read=True, retire_atomic=True, poll_is_wait=True):
     """The served loop's token queue and retirement (search_kernels.cuh,
     namespace sv: `push`, `pop`, `setup_query`, `end_stint`): a bounded
     multi-producer multi-consumer ring in which cell c serves positions
@@ -857,7 +889,9 @@ def serve_token_model(blocks=2, query_blocks=2, cells=2, max_stints=3, pop_by_ca
 
     A block polling an empty ring is a wait (the loop's stall limit would
     end it), so a query whose tokens are all gone without a completion
-    shows up as a deadlock.  Invariants: a pop reads the token pushed for
+    shows up as a deadlock; with `poll_is_wait=False` the poll spins as the
+    device code does, and the same fault is a livelock that only the
+    explorer's progress check finds.  Invariants: a pop reads the token pushed for
     its position; the query completes exactly once, after every token has
     retired; the ring ends empty.  Planted mistakes: claiming by a plain store instead of a CAS, a
     push that does not wait for its cell, a cell freed before its token is
@@ -874,7 +908,7 @@ def serve_token_model(blocks=2, query_blocks=2, cells=2, max_stints=3, pop_by_ca
             if kind == "next":
                 if g.completed:
                     return [("leaves", g, None)]
-                if g.deq >= g.enq:
+                if g.deq >= g.enq and poll_is_wait:
                     return []  # nothing queued: polls until a token comes (or the loop's stall limit)
                 return [(f"reads deq {g.deq}", g, ("seq", g.deq))]
             if kind == "seq":

@@ -258,3 +258,36 @@ def test_serve_rings_taken_is_advisory():
     device may publish `taken` before its copy without harm."""
     res = _run(lm.serve_rings_model(take_after_copy=False))
     assert res.deadlocks == [] and res.finals >= 1
+
+
+# ------------------------------------------------ progress (livelock) check
+@pytest.mark.parametrize("name", ["bottomup", "topdown", "termination", "retrieve", "fifo", "lend", "taker",
+                                  "tokens", "tokens_spin", "rings"])
+def test_every_state_can_finish(name):
+    """Beyond deadlocks: from every reachable state of each protocol some
+    interleaving still finishes, so no cycle of moves can run forever."""
+    model = {
+        "bottomup": lambda: lm.bottomup_park_model(),
+        "topdown": lambda: lm.topdown_handoff_model(),
+        "termination": lambda: lm.termination_model(),
+        "retrieve": lambda: lm.retrieve_steal_model(),
+        "fifo": lambda: lm.fifo_model(),
+        "lend": lambda: lm.owner_lend_model(deletes=4, nodes=2),
+        "taker": lambda: lm.owner_taker_model(),
+        "tokens": lambda: lm.serve_token_model(),
+        "tokens_spin": lambda: lm.serve_token_model(poll_is_wait=False),
+        "rings": lambda: lm.serve_rings_model(),
+    }[name]()
+    init, actors, final = model
+    res = lm.explore(init, actors, final, progress=True)
+    assert res.finals >= 1 and not res.deadlocks and not res.stuck, res.stuck[:1]
+
+
+def test_spinning_retire_by_load_and_store_is_a_livelock():
+    """With the device's spinning poll, the lost completion is no deadlock:
+    the blocks keep polling an empty ring.  Only the progress check sees
+    that no state after the lost write can finish."""
+    init, actors, final = lm.serve_token_model(retire_atomic=False, poll_is_wait=False)
+    res = lm.explore(init, actors, final, progress=True)
+    assert not res.deadlocks and res.stuck
+    assert any("reads tokens 2" in t for t in res.stuck[0])
