@@ -40,7 +40,8 @@ modelled here at the level of those atomic steps:
   search_kernels.cuh, namespace sv): a bounded multi-producer
   multi-consumer ring of per-cell sequence words carries a query's setup
   and search tokens, and the block that retires the last token completes
-  the query; requests and completions cross in rings in pinned host memory.
+  the query; requests and completions cross in rings in pinned host memory,
+  and the host launches the loop again after an idle exit.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -1126,3 +1127,76 @@ def serve_rings_model(queries=4, cap=2, completers=2, guard_by_completions=True,
                    done=tuple((0, -1) for _ in range(cap)), consumed=0, claimed=(-1,) * queries)
     actors = [host, admit_wrap] + [completer(k) for k in range(completers)]
     return (g0, (("idle",), "idle") + ("idle",) * completers), actors, final
+
+
+# --------------------------------------------------------------------------
+# the served device loop's launch, idle exit and relaunch
+
+LoopState = namedtuple("LoopState", "posted taken active completed consumed running armed")
+
+
+def serve_loop_model(requests=2, relaunch_on_poll=True):
+    """The served loop's lifetime (gpuheap_gb300/csrc/serve.cu
+    `gh_serve_poll`, `launch_loop`; search_kernels.cuh `admit`): the device
+    loop leaves after an idle limit with nothing pending or active, and the
+    host launches it again from its poll whenever requests it posted have
+    not all completed.
+
+    * `host`: posts `requests` requests one by one; a poll reads every
+      completion there is, stops once all are read, and otherwise, if the
+      loop's launch has ended, launches it again.
+    * `device` (the admitting block, while launched): takes a posted
+      request (it becomes active), or completes an active one, or, seeing
+      nothing pending or active, arms the idle limit; with the limit armed
+      and the ring still empty when it looks, it decides to leave, and
+      leaves in a later step (the host may post in between).
+
+    Explored with progress=True: from every state every request can still
+    complete.  Planted mistake: a host that launches the loop only when it
+    posts, so that a request posted between the loop's last look at the
+    ring and its exit is stranded."""
+
+    def host(g, pc, trace):
+        moves = []
+        if pc == "run":
+            if g.posted < requests:
+                g2 = _set(g, posted=g.posted + 1)
+                if not relaunch_on_poll and not g.running:
+                    g2 = _set(g2, running=True, armed=False)
+                moves.append((f"posts request {g.posted}", g2, "run"))
+            consumed = g.completed
+            if consumed == requests:
+                moves.append(("reads the last completions: done", _set(g, consumed=consumed), None))
+            else:
+                g2 = _set(g, consumed=consumed)
+                if relaunch_on_poll and not g.running and g.posted > consumed:
+                    moves.append(("poll: loop ended with work left, launches it",
+                                  _set(g2, running=True, armed=False), "run"))
+                elif g2 != g:
+                    moves.append(("poll: reads completions", g2, "run"))
+        return moves
+
+    def device(g, pc, trace):
+        if pc == "leaving":
+            return [("leaves", _set(g, running=False, armed=False), "loop")]
+        if not g.running:
+            return [("done", g, None)] if g.completed == requests else []
+        moves = []
+        if g.posted > g.taken:
+            moves.append(("takes a request", _set(g, taken=g.taken + 1, active=g.active + 1, armed=False), "loop"))
+        if g.active > 0:
+            moves.append(("completes a request", _set(g, active=g.active - 1, completed=g.completed + 1,
+                                                      armed=False), "loop"))
+        if g.active == 0 and g.posted == g.taken:
+            if not g.armed:
+                moves.append(("nothing to do: arms the idle limit", _set(g, armed=True), "loop"))
+            else:
+                moves.append(("idle limit passed, ring empty: decides to leave", g, "leaving"))
+        return moves
+
+    def final(g, trace):
+        if g.completed != requests or g.consumed != requests:
+            raise Violation(f"{g.completed} of {requests} requests completed, {g.consumed} read", trace)
+
+    g0 = LoopState(posted=0, taken=0, active=0, completed=0, consumed=0, running=True, armed=False)
+    return (g0, ("run", "loop")), [host, device], final

@@ -291,3 +291,21 @@ def test_spinning_retire_by_load_and_store_is_a_livelock():
     res = lm.explore(init, actors, final, progress=True)
     assert not res.deadlocks and res.stuck
     assert any("reads tokens 2" in t for t in res.stuck[0])
+
+
+@pytest.mark.parametrize("requests", [1, 2, 3])
+def test_serve_loop_relaunch_never_strands_a_request(requests):
+    """The loop may leave on its idle limit at any time the ring looked
+    empty; the host's poll launches it again while requests are
+    outstanding, so every request completes from every state."""
+    init, actors, final = lm.serve_loop_model(requests=requests)
+    res = lm.explore(init, actors, final, progress=True)
+    assert res.finals >= 1 and not res.deadlocks and not res.stuck
+
+
+def test_serve_loop_relaunch_only_on_post_strands_a_request():
+    init, actors, final = lm.serve_loop_model(relaunch_on_poll=False)
+    res = lm.explore(init, actors, final, progress=True)
+    assert res.stuck and res.deadlocks
+    t = res.deadlocks[0]
+    assert "device:idle limit passed, ring empty: decides to leave" in t and t[-1] == "device:leaves"
