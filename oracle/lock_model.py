@@ -42,6 +42,8 @@ modelled here at the level of those atomic steps:
   and search tokens, and the block that retires the last token completes
   the query; requests and completions cross in rings in pinned host memory,
   and the host launches the loop again after an idle exit.
+* the bulk delete's ticketed turn at node 0 (gpuheap_device.cuh
+  `takeTurn`): blocks take node 0 in the order of their tickets.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -1200,3 +1202,64 @@ def serve_loop_model(requests=2, relaunch_on_poll=True):
 
     g0 = LoopState(posted=0, taken=0, active=0, completed=0, consumed=0, running=True, armed=False)
     return (g0, ("run", "loop")), [host, device], final
+
+
+# --------------------------------------------------------------------------
+# the bulk delete's ticketed turn at node 0
+
+TurnState = namedtuple("TurnState", "ticket serving holder order")
+
+
+def delete_turn_model(blocks=3, rounds=2, pass_after_lock=True, take_ticket=True):
+    """The ticketed turn of a bulk delete's blocks at node 0
+    (include/gpuheap_device.cuh `takeTurn`, `deleteRootImpl` with fair):
+    thread 0 draws t = atomicAdd(delTicket), waits until delServing == t,
+    locks node 0 (a CAS on its lock word, retried while it is held), then
+    passes the turn (delServing = t + 1) and, after its root step, unlocks
+    node 0.  Each block deletes `rounds` times.
+
+    Invariants: node 0 is held by one block at a time, and blocks take it in
+    ticket order -- the fairness the ticket is for (racing on the lock word
+    let one block lose for a whole delete phase).  Planted mistakes: passing
+    the turn before the lock is held (the next ticket then races the lock),
+    and no tickets at all (every block races on the lock word)."""
+
+    def block(i):
+        def act(g, pc, trace):
+            step = pc[0]
+            r = pc[1]
+            nxt_round = ("draw", r + 1) if r + 1 < rounds else None
+            if step == "draw":
+                if not take_ticket:
+                    return [("races for node 0", g, ("lock", r, None))]
+                return [(f"draws ticket {g.ticket}", _set(g, ticket=g.ticket + 1), ("wait", r, g.ticket))]
+            t = pc[2]
+            if step == "wait":
+                if g.serving != t:
+                    return []
+                if pass_after_lock:
+                    return [(f"ticket {t} served", g, ("lock", r, t))]
+                return [(f"ticket {t} served, passes the turn at once", _set(g, serving=t + 1), ("lock_only", r, t))]
+            if step in ("lock", "lock_only"):
+                if g.holder != -1:
+                    return []  # the CAS fails: retry
+                g2 = _set(g, holder=i, order=g.order + ((t if t is not None else i),))
+                if step == "lock" and t is not None:
+                    return [("locks node 0", g2, ("pass", r, t))]
+                return [("locks node 0", g2, ("unlock", r, t))]
+            if step == "pass":
+                return [(f"passes the turn to {t + 1}", _set(g, serving=t + 1), ("unlock", r, t))]
+            if step == "unlock":
+                return [("root step done, unlocks node 0", _set(g, holder=-1), nxt_round)]
+            return []
+        act.__name__ = f"b{i}"
+        return act
+
+    def final(g, trace):
+        if take_ticket and list(g.order) != sorted(g.order):
+            raise Violation(f"node 0 taken in ticket order {list(g.order)}", trace)
+        if len(g.order) != blocks * rounds:
+            raise Violation(f"{len(g.order)} root steps of {blocks * rounds}", trace)
+
+    g0 = TurnState(ticket=0, serving=0, holder=-1, order=())
+    return (g0, tuple(("draw", 0) for _ in range(blocks))), [block(i) for i in range(blocks)], final

@@ -309,3 +309,26 @@ def test_serve_loop_relaunch_only_on_post_strands_a_request():
     assert res.stuck and res.deadlocks
     t = res.deadlocks[0]
     assert "device:idle limit passed, ring empty: decides to leave" in t and t[-1] == "device:leaves"
+
+
+# ------------------------------------------------ bulk delete's ticketed turn
+@pytest.mark.parametrize("blocks,rounds", [(2, 2), (3, 2), (4, 2)])
+def test_delete_turn_is_fifo(blocks, rounds):
+    """Blocks take node 0 in ticket order, one at a time, and never wait forever."""
+    init, actors, final = lm.delete_turn_model(blocks=blocks, rounds=rounds)
+    res = lm.explore(init, actors, final, progress=True)
+    assert res.finals == 1 and not res.deadlocks and not res.stuck
+
+
+def test_delete_turn_passed_before_the_lock_breaks_the_order():
+    with pytest.raises(lm.Violation, match="ticket order"):
+        _run(lm.delete_turn_model(pass_after_lock=False))
+
+
+def test_delete_without_tickets_lets_a_block_lose_every_race():
+    """Racing on the lock word alone: there are runs in which block 0 takes
+    node 0 only after every other block has finished all its rounds."""
+    orders = []
+    init, actors, _ = lm.delete_turn_model(take_ticket=False)
+    lm.explore(init, actors, lambda g, trace: orders.append(g.order))
+    assert any(o[-2:] == (0, 0) and 0 not in o[:-2] for o in orders)
