@@ -44,6 +44,9 @@ modelled here at the level of those atomic steps:
   and the host launches the loop again after an idle exit.
 * the bulk delete's ticketed turn at node 0 (gpuheap_device.cuh
   `takeTurn`): blocks take node 0 in the order of their tickets.
+* top-down bulk inserts into reserved targets (`insertionReserved`,
+  `waitTurn`): they enter the root in target order, or a walk that waits
+  at an earlier insert's unwritten target deadlocks against it.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -1263,3 +1266,88 @@ def delete_turn_model(blocks=3, rounds=2, pass_after_lock=True, take_ticket=True
 
     g0 = TurnState(ticket=0, serving=0, holder=-1, order=())
     return (g0, tuple(("draw", 0) for _ in range(blocks))), [block(i) for i in range(blocks)], final
+
+
+# --------------------------------------------------------------------------
+# top-down reserved bulk inserts: the root in target order
+
+ResvState = namedtuple("ResvState", "status turn written")
+
+
+def reserved_insert_model(targets=5, use_turn=True, pass_after_root=True):
+    """Top-down bulk inserts into reserved targets (include/gpuheap_device.cuh
+    `insertionReserved`, `insert_topdown` with reserved, `waitTurn`;
+    gpuheap_gb300/csrc/heap_kernels.cuh `k_reserve`, `k_mark_reserved`):
+    targets 1..`targets` are drawn at once and their lock words set to
+    TARGET; insert t waits until resvTurn == t, locks the root (node 1;
+    insert 1's target is the root itself), passes the turn (resvTurn = t +
+    1), then walks its path hand over hand -- it locks the next node
+    (waiting while it is INUSE or still an earlier insert's TARGET) before
+    it frees the current one -- and at its target swaps TARGET for INUSE,
+    writes it and frees it.
+
+    Invariants: every target is written once, by its insert, and nobody
+    waits forever.  A walk that meets an earlier insert's unwritten target
+    waits there while holding an ancestor; the earlier insert needs that
+    ancestor too, so the root must be taken in target order.  Planted
+    mistakes: no turn (inserts race for the root), and the turn passed
+    before the root is held."""
+
+    def path(t):
+        p = []
+        x = t
+        while x >= 1:
+            p.append(x)
+            x >>= 1
+        return list(reversed(p))  # 1 .. t
+
+    def ins(t):
+        P = path(t)
+
+        def act(g, pc, trace):
+            step = pc[0]
+            if step == "turn":
+                if use_turn and g.turn != t:
+                    return []
+                if t == 1 or not pass_after_root:
+                    g2 = _set(g, turn=t + 1) if use_turn else g
+                    return [("turn: passes it on" if use_turn else "no turn", g2,
+                             ("at", 0) if t == 1 else ("root", 0))]
+                return [("turn", g, ("root", 0))]
+            if step == "root":
+                if g.status[1] != TD_AVAIL:
+                    return []
+                g2 = _set(g, status=_put(g.status, 1, TD_INUSE))
+                if use_turn and pass_after_root:
+                    g2 = _set(g2, turn=t + 1)
+                return [("locks the root" + (", passes the turn" if use_turn and pass_after_root else ""), g2,
+                         ("at", 0))]
+            if step == "at":
+                k = pc[1]
+                cur = P[k]
+                if cur == t:
+                    if g.status[t] != TD_TARGET:
+                        raise Violation(f"insert {t} found its target in state {g.status[t]}",
+                                        list(trace) + [f"i{t}:at target"])
+                    return [("writes its target", _set(g, status=_put(g.status, t, TD_AVAIL),
+                                                      written=g.written + (t,)), None)]
+                nxt = P[k + 1]
+                if nxt != t:
+                    if g.status[nxt] != TD_AVAIL:
+                        return []
+                    st = _put(_put(g.status, nxt, TD_INUSE), cur, TD_AVAIL)
+                    return [(f"locks {nxt}, frees {cur}", _set(g, status=st), ("at", k + 1))]
+                return [(f"frees {cur}, on to its target", _set(g, status=_put(g.status, cur, TD_AVAIL)),
+                         ("at", k + 1))]
+            return []
+        act.__name__ = f"i{t}"
+        return act
+
+    def final(g, trace):
+        if sorted(g.written) != list(range(1, targets + 1)):
+            raise Violation(f"targets written {g.written}", trace)
+        if any(s != TD_AVAIL for s in g.status[1:]):
+            raise Violation(f"lock words left {g.status[1:]}", trace)
+
+    g0 = ResvState(status=(TD_AVAIL,) + (TD_TARGET,) * targets, turn=1, written=())
+    return (g0, tuple(("turn",) for _ in range(targets))), [ins(t) for t in range(1, targets + 1)], final

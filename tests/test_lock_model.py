@@ -332,3 +332,23 @@ def test_delete_without_tickets_lets_a_block_lose_every_race():
     init, actors, _ = lm.delete_turn_model(take_ticket=False)
     lm.explore(init, actors, lambda g, trace: orders.append(g.order))
     assert any(o[-2:] == (0, 0) and 0 not in o[:-2] for o in orders)
+
+
+# ------------------------------------------------ top-down reserved inserts
+@pytest.mark.parametrize("targets", [3, 5, 7])
+def test_reserved_topdown_inserts_finish(targets):
+    """Reserved targets entered in target order: every target is written
+    once, from every state the inserts can finish."""
+    init, actors, final = lm.reserved_insert_model(targets=targets)
+    res = lm.explore(init, actors, final, progress=True)
+    assert res.finals >= 1 and not res.deadlocks and not res.stuck
+
+
+@pytest.mark.parametrize("mistake", [dict(use_turn=False), dict(pass_after_root=False)])
+def test_reserved_topdown_inserts_out_of_order_deadlock(mistake):
+    """A later target's walk holds an ancestor while it waits at an earlier
+    insert's unwritten target, which needs that ancestor: the root must be
+    entered in target order, and the turn passed only once it is held."""
+    init, actors, final = lm.reserved_insert_model(**mistake)
+    res = lm.explore(init, actors, final, progress=True)
+    assert res.deadlocks and res.stuck
