@@ -1,6 +1,6 @@
 // NVTX ranges around the library's bulk entry points, so that a profiler
-// (`ncu --nvtx --nvtx-include`, Nsight Systems) can attribute each kernel to
-// the call that launched it.  NVTX v3 is header-only; with no tool attached
+// (`ncu --clock-control none --nvtx --nvtx-include ...`, Nsight Systems) can
+// attribute each kernel to the call that launched it.  NVTX v3 is header-only; with no tool attached
 // a push or pop costs a pointer check.
 #pragma once
 #include <nvtx3/nvToolsExt.h>
