@@ -47,6 +47,8 @@ modelled here at the level of those atomic steps:
 * top-down bulk inserts into reserved targets (`insertionReserved`,
   `waitTurn`): they enter the root in target order, or a walk that waits
   at an earlier insert's unwritten target deadlocks against it.
+* the retrieving heap's auxiliary buffer (`RetHeapAux::retrieve`), whose
+  lock is released while a retrieve reads the heap.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -1351,3 +1353,73 @@ def reserved_insert_model(targets=5, use_turn=True, pass_after_root=True):
 
     g0 = ResvState(status=(TD_AVAIL,) + (TD_TARGET,) * targets, turn=1, written=())
     return (g0, tuple(("turn",) for _ in range(targets))), [ins(t) for t in range(1, targets + 1)], final
+
+
+# --------------------------------------------------------------------------
+# the retrieving heap's auxiliary buffer
+
+AuxState = namedtuple("AuxState", "buf lock heap done")
+
+
+def aux_buffer_model(blocks=2, count=2, buffered=(3,), heap_keys=(10, 11, 12, 14), reread_after_relock=True):
+    """gh::RetHeapAux::retrieve (include/gpuheap_retrieve.cuh; reference
+    applications/sssp_longfei_new/heap_with_aux.cuh:48-119): under the
+    buffer's lock a block takes the newest `count` buffered entries, or all
+    of them and then -- with the lock released -- the rest from the heap;
+    it locks again, hands every entry to the check, and appends the ones
+    with work left (here: the even ones) after the buffer's current end.
+
+    Every entry must end in exactly one place: the buffer, the heap, or
+    handed out for good.  Planted mistake: appending after the end the
+    block saw before it released the lock, instead of reading it again
+    (another block's entries appended in between are overwritten)."""
+    work_left = lambda e: e % 2 == 0
+
+    def block(i):
+        def act(g, pc, trace):
+            step = pc[0]
+            if step == "lock":
+                if g.lock != -1:
+                    return []
+                return [("locks the buffer", _set(g, lock=i), ("take",))]
+            if step == "take":
+                have = len(g.buf)
+                if have > count:
+                    got = g.buf[have - count:]
+                    return [(f"takes the newest {got}", _set(g, buf=g.buf[:have - count]), ("check", got, have - count))]
+                got = g.buf
+                if count - have > 0:
+                    return [(f"takes all {got}, unlocks for the heap", _set(g, buf=(), lock=-1), ("heap", got))]
+                return [(f"takes all {got}", _set(g, buf=()), ("check", got, 0))]
+            if step == "heap":
+                got = pc[1]
+                want = count - len(got)
+                more = g.heap[:want]
+                return [(f"retrieves {more} from the heap", _set(g, heap=g.heap[want:]), ("relock", got + more, len(g.buf)))]
+            if step == "relock":
+                if g.lock != -1:
+                    return []
+                end = len(g.buf) if reread_after_relock else 0
+                return [("locks the buffer again", _set(g, lock=i), ("check", pc[1], end))]
+            if step == "check":
+                got, end = pc[1], pc[2]
+                back = tuple(e for e in got if work_left(e))
+                buf = g.buf[:end] + back  # appended after `end`, overwriting what lies there
+                lost = set(g.buf[end:]) - set(back)
+                if lost:
+                    # entries of another block are overwritten
+                    raise Violation(f"block {i} appended at {end} over entries {sorted(lost)}",
+                                    list(trace) + [f"b{i}:append"])
+                done = g.done + tuple(e for e in got if not work_left(e))
+                return [(f"hands out {got}, buffers {back} again", _set(g, buf=buf, done=done, lock=-1), None)]
+            return []
+        act.__name__ = f"b{i}"
+        return act
+
+    def final(g, trace):
+        places = list(g.buf) + list(g.heap) + list(g.done)
+        if sorted(places) != sorted(buffered + heap_keys):
+            raise Violation(f"entries end as buffer {g.buf}, heap {g.heap}, out {g.done}", trace)
+
+    g0 = AuxState(buf=tuple(buffered), lock=-1, heap=tuple(heap_keys), done=())
+    return (g0, tuple(("lock",) for _ in range(blocks))), [block(i) for i in range(blocks)], final

@@ -352,3 +352,21 @@ def test_reserved_topdown_inserts_out_of_order_deadlock(mistake):
     init, actors, final = lm.reserved_insert_model(**mistake)
     res = lm.explore(init, actors, final, progress=True)
     assert res.deadlocks and res.stuck
+
+
+# ------------------------------------------------ retrieving heap's aux buffer
+@pytest.mark.parametrize("blocks,buffered,heap_keys", [(2, (3,), (10, 11, 12, 14)), (3, (3, 4), (10, 11, 12, 13, 14, 16)),
+                                                       (2, (2, 3), (10, 11, 12))])
+def test_aux_buffer_keeps_every_entry(blocks, buffered, heap_keys):
+    """Entries taken, handed to the check and buffered again under the
+    lock (released while the heap is read): each ends in one place."""
+    init, actors, final = lm.aux_buffer_model(blocks=blocks, buffered=buffered, heap_keys=heap_keys)
+    res = lm.explore(init, actors, final, progress=True)
+    assert res.finals >= 1 and not res.deadlocks and not res.stuck
+
+
+def test_aux_buffer_stale_end_overwrites_entries():
+    """Appending at the end seen before the heap read loses the entries
+    another block appended meanwhile."""
+    with pytest.raises(lm.Violation, match="appended at 0 over entries"):
+        _run(lm.aux_buffer_model(reread_after_relock=False))
