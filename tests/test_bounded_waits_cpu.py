@@ -58,3 +58,19 @@ def test_every_polling_loop_is_bounded():
                 unbounded.append(f"{os.path.relpath(path, ROOT)}:{line}: ({cond.strip()[:80]})")
     assert polling >= 20, polling  # the scan sees the device code's polls
     assert not unbounded, "spin-waits without a bound:\n" + "\n".join(unbounded)
+
+
+def test_every_sleeping_loop_is_bounded():
+    """Open loops (for (;;), while (true)) that back off with __nanosleep
+    are waits too: each gives up the same ways."""
+    unbounded = []
+    sleeping = 0
+    for path in SOURCES:
+        for line, cond, loop in _loops(open(path).read()):
+            if cond.strip() not in (";;", "true", "1") or "__nanosleep" not in loop:
+                continue
+            sleeping += 1
+            if not any(b in loop for b in BOUNDS):
+                unbounded.append(f"{os.path.relpath(path, ROOT)}:{line}")
+    assert sleeping >= 5, sleeping
+    assert not unbounded, "sleeping waits without a bound:\n" + "\n".join(unbounded)
