@@ -49,6 +49,8 @@ modelled here at the level of those atomic steps:
   at an earlier insert's unwritten target deadlocks against it.
 * the retrieving heap's auxiliary buffer (`RetHeapAux::retrieve`), whose
   lock is released while a retrieve reads the heap.
+* the FIFO's whole-call push (fifo.cu `k_fifo_bulk_push`): the last block
+  to count itself in publishes what the grid copied.
 
 A spin wait is a step that is enabled only when its condition holds, so a
 state where no actor can move but some have not finished is a deadlock.
@@ -1423,3 +1425,61 @@ def aux_buffer_model(blocks=2, count=2, buffered=(3,), heap_keys=(10, 11, 12, 14
 
     g0 = AuxState(buf=tuple(buffered), lock=-1, heap=tuple(heap_keys), done=())
     return (g0, tuple(("lock",) for _ in range(blocks))), [block(i) for i in range(blocks)], final
+
+
+# --------------------------------------------------------------------------
+# the FIFO's whole-call push: the grid copies, the last block publishes
+
+BulkState = namedtuple("BulkState", "slots arrived write got")
+
+
+def fifo_bulk_model(blocks=3, last_commits=True, arrive_after_copy=True):
+    """k_fifo_bulk_push (gpuheap_gb300/csrc/fifo.cu): one thread reserved
+    positions [0, blocks); block b copies position b, then thread 0 fences
+    and counts itself in (atomicAdd on bulkDone); the block that counts
+    last publishes write = blocks.  A popper reads every position below
+    `write` as soon as it sees it.
+
+    Invariant: a position the popper reads is written.  Planted mistakes:
+    the first block to count in publishes, and a block that counts in
+    before its copy."""
+
+    def block(b):
+        def act(g, pc, trace):
+            if pc == "copy":
+                slots = _put(g.slots, b, True)
+                return [(f"copies position {b}", _set(g, slots=slots), "arrive" if arrive_after_copy else None)]
+            if pc == "arrive":
+                n = g.arrived + 1
+                last = n == blocks if last_commits else n == 1
+                return [(f"counts in ({n})", _set(g, arrived=n), "commit" if last else None)]
+            if pc == "commit":
+                return [("publishes write", _set(g, write=blocks), None)]
+            if pc == "arrive_first":
+                n = g.arrived + 1
+                last = n == blocks
+                return [(f"counts in ({n}) before its copy", _set(g, arrived=n), ("copy_then", last))]
+            if isinstance(pc, tuple) and pc[0] == "copy_then":
+                slots = _put(g.slots, b, True)
+                if pc[1]:
+                    return [(f"copies position {b}", _set(g, slots=slots), "commit")]
+                return [(f"copies position {b}", _set(g, slots=slots), None)]
+            return []
+        act.__name__ = f"b{b}"
+        return act
+
+    def popper(g, pc, trace):
+        k = pc
+        if k >= g.write:
+            return [] if g.write < blocks else [("done", g, None)]
+        if not g.slots[k]:
+            raise Violation(f"popper read position {k} before its block copied it", list(trace) + [f"pop:read {k}"])
+        return [(f"reads position {k}", _set(g, got=g.got + 1), k + 1 if k + 1 < blocks else None)]
+
+    def final(g, trace):
+        if g.got != blocks or g.write != blocks:
+            raise Violation(f"popper read {g.got} of {blocks} (write {g.write})", trace)
+
+    g0 = BulkState(slots=(False,) * blocks, arrived=0, write=0, got=0)
+    start = "copy" if arrive_after_copy else "arrive_first"
+    return (g0, tuple(start for _ in range(blocks)) + (0,)), [block(b) for b in range(blocks)] + [popper], final

@@ -370,3 +370,17 @@ def test_aux_buffer_stale_end_overwrites_entries():
     another block appended meanwhile."""
     with pytest.raises(lm.Violation, match="appended at 0 over entries"):
         _run(lm.aux_buffer_model(reread_after_relock=False))
+
+
+# ------------------------------------------------ FIFO whole-call publish
+@pytest.mark.parametrize("blocks", [2, 3, 4])
+def test_fifo_bulk_publish_after_every_copy(blocks):
+    init, actors, final = lm.fifo_bulk_model(blocks=blocks)
+    res = lm.explore(init, actors, final, progress=True)
+    assert res.finals == 1 and not res.deadlocks and not res.stuck
+
+
+@pytest.mark.parametrize("mistake", [dict(last_commits=False), dict(arrive_after_copy=False)])
+def test_fifo_bulk_early_publish_is_caught(mistake):
+    with pytest.raises(lm.Violation, match="before its block copied it"):
+        _run(lm.fifo_bulk_model(**mistake))
